@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Benchmark of the SPH sub-step on one GB300: particle-updates/s.
+
+Workload (default): the 1,048,576-particle double dambreak — two 64x128x64
+lattice blocks at spacing 2r (r = 0.0025, h = 4r) at opposite corners of the
+box [0,1]^3, jittered by U(+-0.1 spacing) from seed 20171; rest density 1000,
+k = 50 (p = k (rho - rho0)), viscosity 0.01, gravity -9.8, dt = 1e-4.
+
+Printed JSON line (rank 0):
+  value      particle-updates/s with the state resident in HBM: N x K / the
+             summed device time (CUDA events on the solver's stream) of K
+             graph-replayed sub-steps; a 256 MiB buffer is overwritten before
+             every step, outside the timed intervals, so each step starts with
+             a cold L2.
+  e2e        the same metric through the C ABI with host buffers: per step
+             sf_set_state (pinned host AoS pos+vel -> device) + sf_advance_frame
+             + sf_get_state (device -> pinned host), wall clock.
+  roofline   the dominant kernel's algorithmic bytes per launch / its average
+             launch time (CUDA events between stages over K profiled steps),
+             against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (the reference's solver cannot be built: its
+             SPH library is not part of the reference) on the host cores.
+
+``--impl reference`` times that CPU implementation as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-updates/s at 1M (1 GB300); batched vs per-scene; adjoint/forward time"
+UNIT = "particle-updates/s"
+FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+# Algorithmic (compulsory) bytes per particle of each stage: vec3 = 12 B,
+# scalar = 4 B, neighbour reads counted once.  Scan stages are per cell.
+STAGE_BYTES_PER_PARTICLE = {
+    "density": 12 + 8,                       # read pos; write rho, p
+    "force_integrate": 12 + 12 + 8 + 12 + 12 + 8,  # read pos, vel, (p, 1/rho); write pos, vel, key+slot
+    "scatter": 8 + 4 + 4,                    # read key+slot, cell start; write index
+    "rank_gather": 8 + 8 + 24 + 24,          # read key, cell range; read pos+vel; write pos+vel
+}
+STAGE_BYTES_PER_CELL = {"scan_reduce": 4, "scan_tiles": 0, "scan_apply": 4 + 4 + 4}
+STEP_BYTES_PER_UPDATE = 213  # canonical whole-step figure (hash 20 + sort 16 + reorder 48 + cells 5 + density 20 + force 44 + integrate 60)
+
+WORKLOADS = {
+    "double_dambreak_1m": dict(scene=17, particleRadius=0.0025, kernelRadius=0.01),
+    "dambreak_16k": dict(scene=16, particleRadius=0.01, kernelRadius=0.04),
+    "dambreak_64k": dict(scene=19, particleRadius=0.005, kernelRadius=0.02),
+    "sphere_pool": dict(scene=18, particleRadius=0.00227, kernelRadius=0.00908),
+}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [x for x in sm if x >= 0.5 * (mx or max(sm))] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_params(workload: str):
+    from simplefluid_gb300 import SPHParameters
+    w = WORKLOADS[workload]
+    return SPHParameters(particleRadius=w["particleRadius"], kernelRadius=w["kernelRadius"], scene=w["scene"],
+                         pressureStiffness=50.0, viscosity=0.01, restDensity=1000.0, timeStep=1e-4,
+                         boundaryRestitution=0.1)
+
+
+def cpu_oracle_rate(pos: np.ndarray, prm, budget_s: float, max_steps: int, warmup: int = 1):
+    """Oracle sub-steps on the host cores: (updates/s, steps timed, threads)."""
+    from oracle import oracle as O
+    O.build()
+    st = O.State(pos)
+    cp = prm.to_c()
+    if warmup:
+        st.step(cp, warmup)
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        st.step(cp, 1)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return pos.shape[0] * steps / dt, steps, O.max_threads()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def run_reference(args, workload):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from simplefluid_gb300 import scene_positions
+    prm = make_params(workload)
+    pos = scene_positions(prm, prm.scene)
+    budget = min(120.0, max(10.0, 1.0 * args.steps))
+    rate, steps, threads = cpu_oracle_rate(pos, prm, budget, args.steps, warmup=min(args.warmup, 2))
+    sample = (f"{steps} of {args.steps} sub-steps of the {pos.shape[0]}-particle {workload} "
+              f"(after {min(args.warmup, 2)} warm-up), time-bounded at {budget:.0f} s")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": min(args.warmup, 2), "ms_per_step": 1e3 * pos.shape[0] / rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator)",
+        "config": {"workload": workload, "particles": int(pos.shape[0]), "kernel_radius": prm.kernelRadius,
+                   "particle_radius": prm.particleRadius, "dt": prm.timeStep},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "note": "CPU restatement (reference TBB solver library unavailable: not in the reference tree)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, workload):
+    ws, rank, local_rank = dist_env()
+    from simplefluid_gb300 import SPHSolver, scene_positions
+    from simplefluid_gb300 import _capi as C
+    lib = C.load()
+    C.check(lib.sf_select_device(local_rank))
+    prm = make_params(workload)
+    pos = scene_positions(prm, prm.scene)
+    n = pos.shape[0]
+    solver = SPHSolver(prm)
+    solver.setParticles(pos)
+    solver.makeReady()
+    ctx = solver.handle
+
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist_mod
+        torch.cuda.set_device(local_rank)
+        dist_mod.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = dist_mod
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up
+    C.check(lib.sf_step(ctx, max(args.warmup, 3)))
+    solver.synchronize()
+
+    # headline: K graph-replayed sub-steps, cold L2 before each, device time
+    total_ms = ctypes.c_float()
+    step_ms = np.zeros(args.steps, np.float32)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        C.check(lib.sf_step_timed(ctx, args.steps, FLUSH_BYTES, ctypes.byref(total_ms),
+                                  step_ms.ctypes.data_as(ctypes.c_void_p)))
+        # warm-L2 variant, back-to-back (informational)
+        warm_ms = ctypes.c_float()
+        C.check(lib.sf_step_timed(ctx, args.steps, 0, ctypes.byref(warm_ms), None))
+    barrier()
+    t_ms = max_over_ranks(total_ms.value)
+    value = ws * n * args.steps / (t_ms * 1e-3)
+
+    # per-stage device times over K profiled (non-graph) steps
+    nst = lib.sf_stage_count()
+    stage_ms = np.zeros(nst, np.float32)
+    C.check(lib.sf_profile_steps(ctx, args.steps, FLUSH_BYTES, stage_ms.ctypes.data_as(ctypes.c_void_p), nst))
+    names = [lib.sf_stage_name(i).decode() for i in range(nst)]
+    avg_ms = {nm: float(stage_ms[i]) / args.steps for i, nm in enumerate(names)}
+    dom = max(avg_ms, key=avg_ms.get)
+    nx, ny, nz = solver.gridDims()
+    ncells = nx * ny * nz
+    if dom in STAGE_BYTES_PER_PARTICLE:
+        bytes_per_launch = STAGE_BYTES_PER_PARTICLE[dom] * n
+    else:
+        bytes_per_launch = STAGE_BYTES_PER_CELL.get(dom, 0) * ncells
+    peaks = measured_peaks()
+    achieved = bytes_per_launch / (avg_ms[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(workload, {}).get(dom)
+
+    # e2e through the C ABI with pinned host buffers
+    nbytes = n * 3 * 4
+    hp, hv = ctypes.c_void_p(), ctypes.c_void_p()
+    C.check(lib.sf_host_alloc(nbytes, ctypes.byref(hp)))
+    C.check(lib.sf_host_alloc(nbytes, ctypes.byref(hv)))
+    pos_h = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hp.value)).reshape(n, 3)
+    vel_h = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hv.value)).reshape(n, 3)
+    C.check(lib.sf_get_state(ctx, hp, hv, n))
+    dtv = ctypes.c_float()
+    e2e_steps = args.steps
+    for _ in range(max(args.warmup, 3)):
+        C.check(lib.sf_set_state(ctx, hp, hv, n))
+        C.check(lib.sf_advance_frame(ctx, ctypes.byref(dtv)))
+        C.check(lib.sf_get_state(ctx, hp, hv, n))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        C.check(lib.sf_set_state(ctx, hp, hv, n))
+        C.check(lib.sf_advance_frame(ctx, ctypes.byref(dtv)))
+        C.check(lib.sf_get_state(ctx, hp, hv, n))
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    finite = bool(np.isfinite(pos_h).all() and np.isfinite(vel_h).all())
+    lib.sf_host_free(hp)
+    lib.sf_host_free(hv)
+    e2e_value = ws * n * e2e_steps / e2e_s
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, steps, threads = cpu_oracle_rate(pos, prm, args.cpu_seconds, 200)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{steps} sub-steps of the {n}-particle {workload} from its initial state (after 1 warm-up), "
+                         f"CPU oracle with {threads} OpenMP threads; reference TBB solver library unavailable"}
+
+    solver.close()
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    kernels_per_step = nst
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene generator: jittered lattice blocks, seed 20171)",
+        "config": {"workload": workload, "particles": int(n), "kernel_radius": prm.kernelRadius,
+                   "particle_radius": prm.particleRadius, "dt": prm.timeStep, "grid": [nx, ny, nz],
+                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                   "l2": "flushed before every timed step (256 MiB write outside the timed intervals)"},
+        "value_warm_l2": ws * n * args.steps / (max_over_ranks(warm_ms.value) * 1e-3),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "peak_source": peaks["source"], "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "avg_launch_ms": avg_ms[dom],
+                     "step_frac": STEP_BYTES_PER_UPDATE * value / 1e9 / peaks["hbm_gbs"]},
+        "stages_ms": avg_ms,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "path": "sf_set_state(pinned host) + sf_advance_frame + sf_get_state(pinned host)",
+                "state_finite": finite},
+        "gpu_launches": kernels_per_step * args.steps,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="double_dambreak_1m")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, args.workload)
+    else:
+        run_ours(args, args.workload)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/*
+ * sf_capi.h — C ABI of the GB300 SPH step (SimpleFluid drop-in).
+ *
+ * The reference drives its fluid through a C++ template class from an external
+ * solver library:
+ *
+ *   SPHSolver<float>(std::shared_ptr<SPHParameters<float>>)   Include/QtSPHSolver.h:30-31
+ *   void  SPHSolver::makeReady()                              Source/Simulator.cpp:42
+ *   float SPHSolver::advanceFrame()                           Source/Simulator.cpp:49
+ *   QtSPHSolver::getNumParticles/getParticles/getVelocity     Include/QtSPHSolver.h:33-35
+ *   SPHParameters<float> fields + updateParams()              Source/Controller.cpp:54-63
+ *   SceneManager::setupScene*(particles, velocity)            Source/SceneManager.cpp:21-173
+ *
+ * Every entry point below replaces one of those calls with a plain C function:
+ * plain pointers and sizes, no C++ or torch types.  All functions return an
+ * sf_status; on failure sf_last_error() returns a message for the calling
+ * thread.  Host arrays are owned by the caller and copied in or out; the context
+ * owns all device memory.  One context is driven by one host thread at a time;
+ * different contexts are independent.  All device work of a context runs on its
+ * own CUDA stream.
+ *
+ * Particle arrays at this boundary are host AoS float3 (x0 y0 z0 x1 y1 z1 ...),
+ * the layout of the reference's Vec_Vec3<float> (std::vector<glm::vec3>), in the
+ * caller's particle order.
+ */
+#ifndef SF_CAPI_H
+#define SF_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define SF_API __declspec(dllexport)
+#else
+#define SF_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+typedef int sf_status;
+#define SF_OK 0
+#define SF_ERR_INVALID_ARGUMENT 1 /* bad pointer, size or parameter value        */
+#define SF_ERR_CUDA 2             /* a CUDA runtime call failed                  */
+#define SF_ERR_OUT_OF_MEMORY 3    /* device or pinned host allocation failed     */
+#define SF_ERR_NOT_READY 4        /* advance before makeReady / no particles set */
+#define SF_ERR_GRID_TOO_LARGE 5   /* box / kernel radius give too many cells     */
+#define SF_ERR_CAPACITY 6         /* a fixed-size buffer is too small            */
+#define SF_ERR_NO_DEVICE 7        /* no usable CUDA device                       */
+
+/* ---- scenes: SimulationScenes::Scene (Include/Common.h:49-60) ------------ */
+#define SF_SCENE_SPHERE_DROP 0
+#define SF_SCENE_CUBE_DROP 1
+#define SF_SCENE_DAMBREAK 2
+#define SF_SCENE_DOUBLE_DAMBREAK 3
+/* benchmark workloads (box [0,1]^3, sizes fixed by the workload definitions) */
+#define SF_SCENE_DAMBREAK_16K 16        /* 20x40x20 lattice, spacing 0.02          */
+#define SF_SCENE_DOUBLE_DAMBREAK_1M 17  /* two 64x128x64 jittered blocks, r=0.0025 */
+#define SF_SCENE_SPHERE_POOL 18         /* pool of depth 0.3 + sphere R=0.15       */
+#define SF_SCENE_DAMBREAK_64K 19        /* 32x64x32 lattice, r=0.005               */
+
+/* ---- equation of state -------------------------------------------------- */
+#define SF_EOS_LINEAR 0 /* p = k (rho - rho0)            */
+#define SF_EOS_TAIT 1   /* p = k ((rho/rho0)^7 - 1)      */
+
+/*
+ * Parameter block.  The first group is SPHParameters<float> as the reference
+ * GUI writes it (Source/Controller.cpp:54-61) plus particleRadius and scene
+ * (Source/SceneManager.cpp:23,45); the second group holds the constants the
+ * reference leaves inside its solver library, which the benchmark workloads fix.
+ */
+typedef struct sf_params {
+    int32_t num_threads;             /* numThreads; 0 = automatic. Host-side only. */
+    float kernel_radius;             /* kernelRadius h                              */
+    float particle_radius;           /* particleRadius r (lattice spacing 2r)       */
+    float pressure_stiffness;        /* pressureStiffness k                         */
+    float boundary_restitution;      /* boundaryRestitution e in [0,1]              */
+    float viscosity;                 /* viscosity mu                                */
+    float stop_time;                 /* stopTime, seconds of simulated time         */
+    int32_t use_attractive_pressure; /* bUseAttractivePressure: keep p < 0 if set   */
+    int32_t scene;                   /* SF_SCENE_*                                  */
+    float rest_density;              /* rho0                                        */
+    float gravity[3];                /* body acceleration                           */
+    float time_step;                 /* fixed sub-step; advanceFrame returns it     */
+    float box_min[3];                /* simulation box                              */
+    float box_max[3];
+    int32_t eos;                     /* SF_EOS_*                                    */
+    int32_t reserved[3];             /* must be zero                                */
+} sf_params;
+
+typedef struct sf_ctx sf_ctx;
+
+/* ---- errors / version --------------------------------------------------- */
+SF_API const char* sf_last_error(void);
+SF_API const char* sf_version(void);
+
+/* ---- parameters --------------------------------------------------------- */
+/* Fill with the defaults of the 16,000-particle dambreak workload. */
+SF_API sf_status sf_params_default(sf_params* p);
+/* SPHParameters::updateParams() (Source/Controller.cpp:63): validate. */
+SF_API sf_status sf_params_update(sf_params* p);
+
+/* ---- scenes: SceneManager::setupScene (Source/SceneManager.cpp:21-38) --- */
+/* Number of particles the scene generator makes for these parameters. */
+SF_API sf_status sf_scene_count(const sf_params* p, int32_t scene, uint64_t seed, uint32_t* n_out);
+/* Write the scene's positions (and zero velocities) into caller arrays of
+ * capacity `capacity` particles.  vel_xyz may be NULL. */
+SF_API sf_status sf_setup_scene(const sf_params* p, int32_t scene, uint64_t seed, float* pos_xyz,
+                                float* vel_xyz, uint32_t capacity, uint32_t* n_out);
+
+/* ---- device selection ----------------------------------------------------
+ * Make `device` current for the calling thread; contexts created afterwards on
+ * this thread live on it (default: the thread's current device, normally 0). */
+SF_API sf_status sf_select_device(int32_t device);
+
+/* ---- solver lifetime: SPHSolver<float>(params) -------------------------- */
+SF_API sf_status sf_create(const sf_params* p, sf_ctx** out);
+SF_API sf_status sf_destroy(sf_ctx* ctx);
+SF_API sf_status sf_set_params(sf_ctx* ctx, const sf_params* p);
+SF_API sf_status sf_get_params(const sf_ctx* ctx, sf_params* p);
+
+/* ---- particle state: getParticles() / getVelocity() --------------------- */
+/* Copy a host AoS float3 state in.  vel_xyz may be NULL (zero velocity). */
+SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz, uint32_t n);
+/* Copy the state out in the caller's original particle order.  Either output
+ * may be NULL.  Waits for the context's stream. */
+SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint32_t n);
+/* getNumParticles() */
+SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out);
+
+/* ---- stepping: makeReady() / advanceFrame() ----------------------------- */
+/* Build the uniform grid, sort the particles and capture the step graph. */
+SF_API sf_status sf_make_ready(sf_ctx* ctx);
+/* One fixed sub-step; *dt_out receives the simulated time advanced.  The
+ * work is queued on the context's stream; the call does not wait for it. */
+SF_API sf_status sf_advance_frame(sf_ctx* ctx, float* dt_out);
+/* `nsteps` sub-steps, queued as replays of one captured step graph. */
+SF_API sf_status sf_step(sf_ctx* ctx, uint32_t nsteps);
+/* Wait for all queued work of the context. */
+SF_API sf_status sf_synchronize(sf_ctx* ctx);
+/* The context's cudaStream_t, as void*. */
+SF_API sf_status sf_get_stream(sf_ctx* ctx, void** stream_out);
+
+/* ---- pinned host buffers (optional; makes sf_set_state/sf_get_state DMA) - */
+SF_API sf_status sf_host_alloc(size_t bytes, void** ptr_out);
+SF_API sf_status sf_host_free(void* ptr);
+
+/* ---- inspection of the solver's internal (cell-sorted) order ------------
+ * These expose the neighbour-search structures so that callers and tests
+ * can check them; they wait for the stream. */
+/* Grid dimensions (cells per axis) of the context's uniform grid. */
+SF_API sf_status sf_get_grid(const sf_ctx* ctx, uint32_t dims_out[3]);
+/* Sorted state: pos4/vel4 are n*4 floats (w of pos4 is 0), ids are the
+ * caller's original indices, keys the linear cell keys.  Any may be NULL. */
+SF_API sf_status sf_get_sorted(sf_ctx* ctx, float* pos4, float* vel4, uint32_t* ids, uint32_t* keys,
+                               uint32_t n);
+/* cell_start has ncells+1 entries: particles of cell c are [cs[c], cs[c+1]). */
+SF_API sf_status sf_get_cell_start(sf_ctx* ctx, uint32_t* cell_start, uint32_t count);
+/* Run the density pass on the current sorted state and return rho and p in
+ * sorted order.  Either output may be NULL. */
+SF_API sf_status sf_compute_density(sf_ctx* ctx, float* rho, float* pressure, uint32_t n);
+/* Run density + forces on the current sorted state without integrating and
+ * return the acceleration (n*3 floats, sorted order). */
+SF_API sf_status sf_compute_accel(sf_ctx* ctx, float* accel_xyz, uint32_t n);
+/* Per sorted particle: number of neighbours j != i with |xi-xj|^2 < h^2 and a
+ * order-independent hash of their original indices. */
+SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash, uint32_t n);
+
+/* ---- measurement ----------------------------------------------------------
+ * Device-side timing with CUDA events on the context's stream.  Not part of
+ * the reference interface (which has none); used by benchmarks. */
+/* Run `nsteps` sub-steps (graph replays).  With flush_bytes > 0 a scratch
+ * buffer of that size is overwritten before every step, outside the timed
+ * intervals, to evict the L2 cache.  *total_ms receives the summed device time
+ * of the steps; step_ms (may be NULL) receives each step's time. */
+SF_API sf_status sf_step_timed(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* total_ms,
+                               float* step_ms);
+/* Number of kernel stages in one sub-step and their names. */
+SF_API uint32_t sf_stage_count(void);
+SF_API const char* sf_stage_name(uint32_t stage);
+/* Run `nsteps` sub-steps stage by stage (no graph) with an event between
+ * stages; stage_ms[s] receives the summed device time of stage s over all
+ * steps (nstages must equal sf_stage_count()). */
+SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
+                                  uint32_t nstages);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SF_CAPI_H */

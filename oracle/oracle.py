@@ -1,0 +1,178 @@
+"""ctypes wrapper of the CPU oracle (oracle/sph_oracle.cpp) — TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use
+it, as the checker.  The product package never imports this module.
+
+Parity with the reference's solver library (Banana SPHSolver, absent from the
+reference tree) is unpinned; the scene generators are pinned against the
+reference's own Source/SceneManager.cpp compiled by build_ref.sh.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_int, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+from simplefluid_gb300._capi import sf_params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "libsf_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_scenes.so")
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(ORACLE_LIB):
+        subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")])
+    return ORACLE_LIB
+
+
+def build_ref() -> str | None:
+    """Compile the reference scene generator when the reference tree is here."""
+    try:
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")],
+                              stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    except (subprocess.CalledProcessError, OSError):
+        return None
+    return REF_LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            build()
+        l = ctypes.CDLL(ORACLE_LIB)
+        P = POINTER(sf_params)
+        l.sfo_derive.argtypes = [P, c_void_p]
+        l.sfo_scene.argtypes = [P, c_int, c_uint64, c_void_p, c_uint32, POINTER(c_uint32)]
+        for sfx in ("f32", "f64"):
+            getattr(l, f"sfo_sort_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+            getattr(l, f"sfo_density_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
+            getattr(l, f"sfo_accel_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+            getattr(l, f"sfo_integrate_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p]
+            getattr(l, f"sfo_neighbour_stats_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
+            getattr(l, f"sfo_step_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_uint32, c_int]
+        l.sfo_max_threads.argtypes = []
+        _lib = l
+    return _lib
+
+
+def ref_lib() -> ctypes.CDLL | None:
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB):
+        r = ctypes.CDLL(REF_LIB)
+        r.ref_setup_scene.argtypes = [c_int, ctypes.c_float, c_void_p, c_uint32, POINTER(c_uint32)]
+        _ref = r
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(c_void_p)
+
+
+def _chk(st: int, what: str) -> None:
+    if st != 0:
+        raise RuntimeError(f"oracle {what} failed with status {st}")
+
+
+def derive(p: sf_params) -> dict:
+    out = np.zeros(16, np.float64)
+    _chk(lib().sfo_derive(ctypes.byref(p), _ptr(out)), "derive")
+    keys = ["h", "h2", "mass", "cd", "cp", "cv", "lo0", "lo1", "lo2", "hi0", "hi1", "hi2", "nx", "ny", "nz", "ncells"]
+    return dict(zip(keys, out.tolist()))
+
+
+def scene(p: sf_params, scene_id: int, seed: int = 20171) -> np.ndarray:
+    n = c_uint32(0)
+    _chk(lib().sfo_scene(ctypes.byref(p), scene_id, seed, None, 0, ctypes.byref(n)), "scene count")
+    out = np.zeros((n.value, 3), np.float32)
+    _chk(lib().sfo_scene(ctypes.byref(p), scene_id, seed, _ptr(out), n.value, ctypes.byref(n)), "scene")
+    return out
+
+
+def ref_scene(scene_id: int, particle_radius: float) -> np.ndarray | None:
+    """Positions from the reference's own SceneManager (None if not built)."""
+    r = ref_lib()
+    if r is None:
+        return None
+    n = c_uint32(0)
+    _chk(r.ref_setup_scene(scene_id, particle_radius, None, 0, ctypes.byref(n)), "ref scene count")
+    out = np.zeros((n.value, 3), np.float32)
+    _chk(r.ref_setup_scene(scene_id, particle_radius, _ptr(out), n.value, ctypes.byref(n)), "ref scene")
+    return out
+
+
+class State:
+    """Particle state in the oracle's current (sorted-after-step) order."""
+
+    def __init__(self, pos, vel=None, dtype=np.float32):
+        self.dtype = np.dtype(dtype)
+        self.pos = np.ascontiguousarray(pos, dtype=self.dtype).reshape(-1, 3).copy()
+        n = self.pos.shape[0]
+        self.vel = (np.zeros((n, 3), self.dtype) if vel is None
+                    else np.ascontiguousarray(vel, dtype=self.dtype).reshape(-1, 3).copy())
+        self.ids = np.arange(n, dtype=np.uint32)
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+    @property
+    def sfx(self) -> str:
+        return "f32" if self.dtype == np.float32 else "f64"
+
+    def sort(self, p: sf_params, want_cells: bool = False):
+        d = derive(p)
+        keys = np.zeros(self.n, np.uint32)
+        cs = np.zeros(int(d["ncells"]) + 1, np.uint32) if want_cells else None
+        _chk(getattr(lib(), f"sfo_sort_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel),
+                                                    _ptr(self.ids), _ptr(keys), _ptr(cs)), "sort")
+        return keys, cs
+
+    def density(self, p: sf_params):
+        rho = np.zeros(self.n, self.dtype)
+        prs = np.zeros(self.n, self.dtype)
+        inv = np.zeros(self.n, self.dtype)
+        _chk(getattr(lib(), f"sfo_density_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(rho),
+                                                       _ptr(prs), _ptr(inv)), "density")
+        return rho, prs, inv
+
+    def accel(self, p: sf_params, prs=None, inv=None):
+        if prs is None:
+            _, prs, inv = self.density(p)
+        acc = np.zeros((self.n, 3), self.dtype)
+        _chk(getattr(lib(), f"sfo_accel_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel),
+                                                     _ptr(prs), _ptr(inv), _ptr(acc)), "accel")
+        return acc
+
+    def integrate(self, p: sf_params, acc):
+        acc = np.ascontiguousarray(acc, self.dtype)
+        _chk(getattr(lib(), f"sfo_integrate_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel),
+                                                         _ptr(acc)), "integrate")
+
+    def neighbour_stats(self, p: sf_params):
+        cnt = np.zeros(self.n, np.uint32)
+        hsh = np.zeros(self.n, np.uint32)
+        _chk(getattr(lib(), f"sfo_neighbour_stats_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos),
+                                                               _ptr(self.ids), _ptr(cnt), _ptr(hsh)), "nbr")
+        return cnt, hsh
+
+    def step(self, p: sf_params, nsteps: int = 1, threads: int = 0):
+        _chk(getattr(lib(), f"sfo_step_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel),
+                                                    _ptr(self.ids), nsteps, threads), "step")
+
+    def original_order(self):
+        """Positions and velocities in the caller's original particle order."""
+        inv = np.empty_like(self.ids)
+        inv[self.ids] = np.arange(self.n, dtype=np.uint32)
+        return self.pos[inv], self.vel[inv]
+
+
+def max_threads() -> int:
+    return int(lib().sfo_max_threads())

@@ -1,0 +1,19 @@
+"""SimpleFluid SPH step on one GB300 (sm_103a), behind the reference's solver interface.
+
+The compute lives in the in-tree CUDA library ``_lib/libsimplefluid_gb300.so``
+(C ABI: include/sf_capi.h); this package is the host-side mirror of the
+reference's ``SPHParameters`` / ``SPHSolver`` / ``SceneManager`` / ``Simulator``.
+"""
+from ._capi import SFError, load  # noqa: F401
+from .solver import (  # noqa: F401
+    FRAME_TIME,
+    SceneManager,
+    Simulator,
+    SPHParameters,
+    SPHSolver,
+    scene_positions,
+    substeps_per_frame,
+)
+
+__all__ = ["SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
+           "substeps_per_frame", "FRAME_TIME", "load"]

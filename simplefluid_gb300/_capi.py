@@ -1,0 +1,131 @@
+"""ctypes binding of the C ABI declared in include/sf_capi.h.
+
+The shared library is built in-tree (``simplefluid_gb300/_lib``) by
+``simplefluid_gb300.build``.  Loading fails loudly when it is missing: there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libsimplefluid_gb300.so")
+
+SF_OK = 0
+SF_ERR_INVALID_ARGUMENT = 1
+SF_ERR_CUDA = 2
+SF_ERR_OUT_OF_MEMORY = 3
+SF_ERR_NOT_READY = 4
+SF_ERR_GRID_TOO_LARGE = 5
+SF_ERR_CAPACITY = 6
+SF_ERR_NO_DEVICE = 7
+
+SF_SCENE_SPHERE_DROP = 0
+SF_SCENE_CUBE_DROP = 1
+SF_SCENE_DAMBREAK = 2
+SF_SCENE_DOUBLE_DAMBREAK = 3
+SF_SCENE_DAMBREAK_16K = 16
+SF_SCENE_DOUBLE_DAMBREAK_1M = 17
+SF_SCENE_SPHERE_POOL = 18
+SF_SCENE_DAMBREAK_64K = 19
+
+SF_EOS_LINEAR = 0
+SF_EOS_TAIT = 1
+
+
+class sf_params(ctypes.Structure):
+    """Mirror of ``struct sf_params`` (include/sf_capi.h)."""
+
+    _fields_ = [
+        ("num_threads", c_int32),
+        ("kernel_radius", c_float),
+        ("particle_radius", c_float),
+        ("pressure_stiffness", c_float),
+        ("boundary_restitution", c_float),
+        ("viscosity", c_float),
+        ("stop_time", c_float),
+        ("use_attractive_pressure", c_int32),
+        ("scene", c_int32),
+        ("rest_density", c_float),
+        ("gravity", c_float * 3),
+        ("time_step", c_float),
+        ("box_min", c_float * 3),
+        ("box_max", c_float * 3),
+        ("eos", c_int32),
+        ("reserved", c_int32 * 3),
+    ]
+
+
+class SFError(RuntimeError):
+    """Raised when a C-ABI call returns a non-zero sf_status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"sf_status {status}: {message}")
+        self.status = status
+
+
+_P = POINTER
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "sf_last_error": (c_char_p, []),
+    "sf_version": (c_char_p, []),
+    "sf_params_default": (c_int32, [_P(sf_params)]),
+    "sf_params_update": (c_int32, [_P(sf_params)]),
+    "sf_scene_count": (c_int32, [_P(sf_params), c_int32, c_uint64, _P(c_uint32)]),
+    "sf_setup_scene": (c_int32, [_P(sf_params), c_int32, c_uint64, c_void_p, c_void_p, c_uint32, _P(c_uint32)]),
+    "sf_select_device": (c_int32, [c_int32]),
+    "sf_create": (c_int32, [_P(sf_params), _P(c_void_p)]),
+    "sf_destroy": (c_int32, [c_void_p]),
+    "sf_set_params": (c_int32, [c_void_p, _P(sf_params)]),
+    "sf_get_params": (c_int32, [c_void_p, _P(sf_params)]),
+    "sf_set_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_get_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_get_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
+    "sf_make_ready": (c_int32, [c_void_p]),
+    "sf_advance_frame": (c_int32, [c_void_p, _P(c_float)]),
+    "sf_step": (c_int32, [c_void_p, c_uint32]),
+    "sf_synchronize": (c_int32, [c_void_p]),
+    "sf_get_stream": (c_int32, [c_void_p, _P(c_void_p)]),
+    "sf_host_alloc": (c_int32, [c_size_t, _P(c_void_p)]),
+    "sf_host_free": (c_int32, [c_void_p]),
+    "sf_get_grid": (c_int32, [c_void_p, c_void_p]),
+    "sf_get_sorted": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_get_cell_start": (c_int32, [c_void_p, c_void_p, c_uint32]),
+    "sf_compute_density": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_compute_accel": (c_int32, [c_void_p, c_void_p, c_uint32]),
+    "sf_neighbour_stats": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_step_timed": (c_int32, [c_void_p, c_uint32, c_uint64, _P(c_float), c_void_p]),
+    "sf_stage_count": (c_uint32, []),
+    "sf_stage_name": (c_char_p, [c_uint32]),
+    "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the in-tree C-ABI library; raise if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"SimpleFluid GB300 library not built: {p} is missing "
+            "(run `python -c 'import __graft_entry__ as g; g.build()'`)")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != SF_OK:
+        msg = load().sf_last_error()
+        raise SFError(status, msg.decode() if msg else "")

@@ -1,0 +1,730 @@
+// sf_capi.cpp — the C ABI (include/sf_capi.h): solver contexts, device
+// memory, the captured step graph, host<->device state copies.
+//
+// Maps the reference's solver calls onto one CUDA stream per context:
+//   SPHSolver<float>(params)        Include/QtSPHSolver.h:30-31   -> sf_create
+//   makeReady()                     Source/Simulator.cpp:42       -> sf_make_ready
+//   advanceFrame()                  Source/Simulator.cpp:49       -> sf_advance_frame / sf_step
+//   getParticles()/getVelocity()    Include/QtSPHSolver.h:34-35   -> sf_get_state / sf_set_state
+//   SceneManager::setupScene        Source/SceneManager.cpp:21-38 -> sf_setup_scene
+//   SPHParameters::updateParams()   Source/Controller.cpp:63      -> sf_params_update
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sf_internal.h"
+
+struct sf_ctx {
+    sf_params params{};
+    sf::SimConst c{};
+    sf::DeviceState d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t step_graph = nullptr;
+    bool sorted = false;  // particles uploaded and cell-sorted
+    float* h_stage = nullptr;  // pinned staging for pageable caller buffers
+    size_t h_stage_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+sf_status fail(sf_status st, const std::string& msg) {
+    g_error = msg;
+    return st;
+}
+
+sf_status cuda_fail(cudaError_t e, const char* what) {
+    cudaGetLastError();  // clear a sticky launch error where possible
+    return fail(e == cudaErrorMemoryAllocation ? SF_ERR_OUT_OF_MEMORY : SF_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SF_CUDA(call)                                      \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+#define SF_TRY(call)                    \
+    do {                                \
+        sf_status st_ = (call);         \
+        if (st_ != SF_OK) return st_;   \
+    } while (0)
+
+constexpr uint64_t kMaxCells = 1ull << 28;
+
+sf_status validate(const sf_params& p) {
+    auto finite = [](float v) { return std::isfinite(v); };
+    if (!finite(p.kernel_radius) || !(p.kernel_radius > 0.f))
+        return fail(SF_ERR_INVALID_ARGUMENT, "kernel_radius must be positive and finite");
+    if (!finite(p.particle_radius) || !(p.particle_radius > 0.f))
+        return fail(SF_ERR_INVALID_ARGUMENT, "particle_radius must be positive and finite");
+    if (!finite(p.pressure_stiffness) || p.pressure_stiffness < 0.f)
+        return fail(SF_ERR_INVALID_ARGUMENT, "pressure_stiffness must be >= 0");
+    if (!finite(p.viscosity) || p.viscosity < 0.f) return fail(SF_ERR_INVALID_ARGUMENT, "viscosity must be >= 0");
+    if (!finite(p.boundary_restitution) || p.boundary_restitution < 0.f || p.boundary_restitution > 1.f)
+        return fail(SF_ERR_INVALID_ARGUMENT, "boundary_restitution must be in [0, 1]");
+    if (!finite(p.rest_density) || !(p.rest_density > 0.f))
+        return fail(SF_ERR_INVALID_ARGUMENT, "rest_density must be positive");
+    if (!finite(p.time_step) || !(p.time_step > 0.f)) return fail(SF_ERR_INVALID_ARGUMENT, "time_step must be > 0");
+    if (!finite(p.stop_time) || p.stop_time < 0.f) return fail(SF_ERR_INVALID_ARGUMENT, "stop_time must be >= 0");
+    if (p.eos != SF_EOS_LINEAR && p.eos != SF_EOS_TAIT) return fail(SF_ERR_INVALID_ARGUMENT, "unknown eos");
+    if (p.num_threads < 0) return fail(SF_ERR_INVALID_ARGUMENT, "num_threads must be >= 0");
+    if (p.reserved[0] || p.reserved[1] || p.reserved[2])
+        return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    for (int a = 0; a < 3; ++a) {
+        if (!finite(p.gravity[a]) || !finite(p.box_min[a]) || !finite(p.box_max[a]))
+            return fail(SF_ERR_INVALID_ARGUMENT, "gravity and box must be finite");
+        if (!((double)p.box_max[a] - p.box_min[a] > 2.0 * p.particle_radius))
+            return fail(SF_ERR_INVALID_ARGUMENT, "box must be wider than one particle diameter on every axis");
+    }
+    return SF_OK;
+}
+
+sf_status ensure_stage(sf_ctx* ctx, size_t bytes) {
+    if (ctx->h_stage_bytes >= bytes) return SF_OK;
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_bytes = 0;
+    SF_CUDA(cudaMallocHost(&ctx->h_stage, bytes));
+    ctx->h_stage_bytes = bytes;
+    return SF_OK;
+}
+
+bool is_pinned(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+void free_particles(sf::DeviceState& d) {
+    void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    d.pos = d.vel = d.pos2 = d.vel2 = d.accel = nullptr;
+    d.pr = nullptr;
+    d.rho = nullptr;
+    d.key_slot = nullptr;
+    d.tmp = nullptr;
+    d.io = nullptr;
+    d.cap = 0;
+}
+
+void free_grid(sf::DeviceState& d) {
+    if (d.counts) cudaFree(d.counts);
+    if (d.cell_start) cudaFree(d.cell_start);
+    if (d.tile_sums) cudaFree(d.tile_sums);
+    d.counts = d.cell_start = d.tile_sums = nullptr;
+    d.ncells = d.ncells_pad = d.ntiles = 0;
+}
+
+void drop_graph(sf_ctx* ctx) {
+    if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
+    ctx->step_graph = nullptr;
+}
+
+sf_status alloc_grid(sf_ctx* ctx) {
+    sf::DeviceState& d = ctx->d;
+    if (d.ncells == ctx->c.ncells && d.counts) return SF_OK;
+    free_grid(d);
+    const uint64_t pad = ((uint64_t)ctx->c.ncells + 1 + sf::kScanTile - 1) / sf::kScanTile * sf::kScanTile;
+    d.ncells = ctx->c.ncells;
+    d.ncells_pad = (uint32_t)pad;
+    d.ntiles = (uint32_t)(pad / sf::kScanTile);
+    SF_CUDA(cudaMalloc(&d.counts, pad * sizeof(uint32_t)));
+    SF_CUDA(cudaMalloc(&d.cell_start, pad * sizeof(uint32_t)));
+    SF_CUDA(cudaMalloc(&d.tile_sums, (size_t)d.ntiles * sizeof(uint32_t)));
+    SF_CUDA(cudaMemsetAsync(d.counts, 0, pad * sizeof(uint32_t), ctx->stream));
+    SF_CUDA(cudaMemsetAsync(d.cell_start, 0, pad * sizeof(uint32_t), ctx->stream));
+    return SF_OK;
+}
+
+sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
+    sf::DeviceState& d = ctx->d;
+    if (n <= d.cap && d.pos) return SF_OK;
+    free_particles(d);
+    const size_t c = n ? n : 1;
+    SF_CUDA(cudaMalloc(&d.pos, c * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&d.vel, c * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&d.pos2, c * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&d.vel2, c * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&d.pr, c * sizeof(float2)));
+    SF_CUDA(cudaMalloc(&d.rho, c * sizeof(float)));
+    SF_CUDA(cudaMalloc(&d.key_slot, c * sizeof(uint2)));
+    SF_CUDA(cudaMalloc(&d.tmp, c * sizeof(uint32_t)));
+    SF_CUDA(cudaMalloc(&d.io, c * 6 * sizeof(float)));
+    d.cap = (uint32_t)c;
+    return SF_OK;
+}
+
+sf_status set_device(const sf_ctx* ctx) {
+    SF_CUDA(cudaSetDevice(ctx->device));
+    return SF_OK;
+}
+
+sf_status check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return SF_OK;
+}
+
+// Upload n particles (device AoS staging already filled) and cell-sort them.
+sf_status sort_uploaded(sf_ctx* ctx) {
+    sf::DeviceState& d = ctx->d;
+    sf::launch_load_aos(d.io, d.io + 3 * (size_t)d.n, d.n, d.pos2, d.vel2, ctx->stream);
+    sf::launch_hash_count(d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
+    sf::enqueue_sort_tail(d, ctx->stream);
+    SF_TRY(check_launch("initial sort"));
+    ctx->sorted = true;
+    return SF_OK;
+}
+
+sf_status capture_step(sf_ctx* ctx) {
+    drop_graph(ctx);
+    cudaGraph_t g = nullptr;
+    SF_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    sf::enqueue_step(ctx->d, ctx->c, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(step)");
+    e = cudaGraphInstantiate(&ctx->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        ctx->step_graph = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate(step)");
+    }
+    return SF_OK;
+}
+
+sf_status need_ctx(const sf_ctx* ctx) {
+    if (!ctx) return fail(SF_ERR_INVALID_ARGUMENT, "null context");
+    return SF_OK;
+}
+
+sf_status need_sorted(const sf_ctx* ctx) {
+    SF_TRY(need_ctx(ctx));
+    if (!ctx->sorted || ctx->d.n == 0) return fail(SF_ERR_NOT_READY, "no particles: call sf_set_state first");
+    return SF_OK;
+}
+
+// Device -> host copy into a caller buffer (direct when pinned).
+sf_status copy_out(sf_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return SF_OK;
+    if (is_pinned(dst)) {
+        SF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
+    SF_TRY(ensure_stage(ctx, bytes));
+    SF_CUDA(cudaMemcpyAsync(ctx->h_stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(dst, ctx->h_stage, bytes);
+    return SF_OK;
+}
+
+sf_status copy_in(sf_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return SF_OK;
+    if (is_pinned(src)) {
+        SF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        return SF_OK;
+    }
+    SF_TRY(ensure_stage(ctx, bytes));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));  // staging may still feed an earlier copy
+    std::memcpy(ctx->h_stage, src, bytes);
+    SF_CUDA(cudaMemcpyAsync(dst, ctx->h_stage, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return SF_OK;
+}
+
+}  // namespace
+
+namespace sf {
+
+int derive_constants(const sf_params& p, SimConst* c, const char** why) {
+    const double h = p.kernel_radius, r = p.particle_radius;
+    const double kPi = 3.14159265358979323846;
+    const double mass = (double)p.rest_density * (2.0 * r) * (2.0 * r) * (2.0 * r);
+    const double h3 = h * h * h, h6 = h3 * h3, h9 = h6 * h3;
+    c->h = (float)h;
+    c->h2 = (float)(h * h);
+    c->mass = (float)mass;
+    c->cd = (float)(mass * 315.0 / (64.0 * kPi * h9));
+    c->cp = (float)(mass * 45.0 / (kPi * h6) * 0.5);
+    c->cv = (float)((double)p.viscosity * mass * 45.0 / (kPi * h6));
+    c->k = p.pressure_stiffness;
+    c->rho0 = p.rest_density;
+    c->inv_rho0 = (float)(1.0 / (double)p.rest_density);
+    c->dt = p.time_step;
+    c->e = p.boundary_restitution;
+    c->eos = p.eos;
+    c->attractive = p.use_attractive_pressure ? 1 : 0;
+    uint64_t cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        const double ext = (double)p.box_max[a] - (double)p.box_min[a];
+        c->g[a] = p.gravity[a];
+        c->lo[a] = (float)((double)p.box_min[a] + r);
+        c->hi[a] = (float)((double)p.box_max[a] - r);
+        c->bmin[a] = p.box_min[a];
+        double na = std::floor(ext / h);
+        if (na < 1) na = 1;
+        if (na > 65535) {
+            *why = "more than 65535 cells along one axis (box / kernel_radius too large)";
+            return SF_ERR_GRID_TOO_LARGE;
+        }
+        c->n[a] = (int)na;
+        c->inv_cell[a] = (float)(na / ext);
+        cells *= (uint64_t)c->n[a];
+    }
+    if (cells > kMaxCells) {
+        *why = "uniform grid would exceed 2^28 cells (box / kernel_radius too large)";
+        return SF_ERR_GRID_TOO_LARGE;
+    }
+    c->ncells = (uint32_t)cells;
+    return SF_OK;
+}
+
+}  // namespace sf
+
+// =====================================================================
+extern "C" {
+
+SF_API const char* sf_last_error(void) { return g_error.c_str(); }
+
+SF_API const char* sf_version(void) { return "simplefluid-gb300 0.1 (sm_103a)"; }
+
+SF_API sf_status sf_params_default(sf_params* p) {
+    if (!p) return fail(SF_ERR_INVALID_ARGUMENT, "null params");
+    std::memset(p, 0, sizeof(*p));
+    p->num_threads = 0;
+    p->particle_radius = 0.01f;
+    p->kernel_radius = 0.04f;
+    p->pressure_stiffness = 50.0f;
+    p->boundary_restitution = 0.1f;
+    p->viscosity = 0.01f;
+    p->stop_time = 5.0f;
+    p->use_attractive_pressure = 0;
+    p->scene = SF_SCENE_DAMBREAK_16K;
+    p->rest_density = 1000.0f;
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -9.8f;
+    p->gravity[2] = 0.0f;
+    p->time_step = 1e-4f;
+    for (int a = 0; a < 3; ++a) {
+        p->box_min[a] = 0.0f;
+        p->box_max[a] = 1.0f;
+    }
+    p->eos = SF_EOS_LINEAR;
+    return SF_OK;
+}
+
+SF_API sf_status sf_params_update(sf_params* p) {
+    if (!p) return fail(SF_ERR_INVALID_ARGUMENT, "null params");
+    SF_TRY(validate(*p));
+    sf::SimConst c;
+    const char* why = "";
+    const int st = sf::derive_constants(*p, &c, &why);
+    if (st) return fail(st, why);
+    return SF_OK;
+}
+
+SF_API sf_status sf_scene_count(const sf_params* p, int32_t scene, uint64_t seed, uint32_t* n_out) {
+    if (!p || !n_out) return fail(SF_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<float> pts;
+    const char* why = "";
+    const int st = sf::scene_points(*p, scene, seed, pts, &why);
+    if (st) return fail(st, why);
+    *n_out = (uint32_t)(pts.size() / 3);
+    return SF_OK;
+}
+
+SF_API sf_status sf_setup_scene(const sf_params* p, int32_t scene, uint64_t seed, float* pos_xyz, float* vel_xyz,
+                                uint32_t capacity, uint32_t* n_out) {
+    if (!p || !pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<float> pts;
+    const char* why = "";
+    const int st = sf::scene_points(*p, scene, seed, pts, &why);
+    if (st) return fail(st, why);
+    const uint32_t n = (uint32_t)(pts.size() / 3);
+    if (n_out) *n_out = n;
+    if (n > capacity) return fail(SF_ERR_CAPACITY, "scene has more particles than the output capacity");
+    std::memcpy(pos_xyz, pts.data(), pts.size() * sizeof(float));
+    if (vel_xyz) std::memset(vel_xyz, 0, pts.size() * sizeof(float));
+    return SF_OK;
+}
+
+SF_API sf_status sf_select_device(int32_t device) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SF_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= ndev) return fail(SF_ERR_INVALID_ARGUMENT, "device index out of range");
+    SF_CUDA(cudaSetDevice(device));
+    return SF_OK;
+}
+
+SF_API sf_status sf_create(const sf_params* p, sf_ctx** out) {
+    if (!p || !out) return fail(SF_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    SF_TRY(validate(*p));
+    sf::SimConst c;
+    const char* why = "";
+    int st = sf::derive_constants(*p, &c, &why);
+    if (st) return fail(st, why);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SF_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    sf_ctx* ctx = new sf_ctx();
+    ctx->params = *p;
+    ctx->c = c;
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return cuda_fail(e, "stream creation");
+    }
+    st = alloc_grid(ctx);
+    if (st) {
+        sf_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return SF_OK;
+}
+
+SF_API sf_status sf_destroy(sf_ctx* ctx) {
+    if (!ctx) return SF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    free_particles(ctx->d);
+    free_grid(ctx->d);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SF_OK;
+}
+
+SF_API sf_status sf_set_params(sf_ctx* ctx, const sf_params* p) {
+    SF_TRY(need_ctx(ctx));
+    if (!p) return fail(SF_ERR_INVALID_ARGUMENT, "null params");
+    SF_TRY(validate(*p));
+    sf::SimConst c;
+    const char* why = "";
+    const int st = sf::derive_constants(*p, &c, &why);
+    if (st) return fail(st, why);
+    SF_TRY(set_device(ctx));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    const bool grid_changed = std::memcmp(c.n, ctx->c.n, sizeof(c.n)) != 0 ||
+                              std::memcmp(c.bmin, ctx->c.bmin, sizeof(c.bmin)) != 0 ||
+                              std::memcmp(c.inv_cell, ctx->c.inv_cell, sizeof(c.inv_cell)) != 0;
+    ctx->params = *p;
+    ctx->c = c;
+    drop_graph(ctx);
+    if (grid_changed) {
+        SF_TRY(alloc_grid(ctx));
+        if (ctx->sorted && ctx->d.n) {
+            // Re-bucket the current state on the new grid (positions unchanged).
+            sf::DeviceState& d = ctx->d;
+            SF_CUDA(cudaMemcpyAsync(d.pos2, d.pos, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                    ctx->stream));
+            SF_CUDA(cudaMemcpyAsync(d.vel2, d.vel, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                    ctx->stream));
+            sf::launch_hash_count(d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
+            sf::enqueue_sort_tail(d, ctx->stream);
+            SF_TRY(check_launch("re-sort after parameter change"));
+        }
+    }
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_params(const sf_ctx* ctx, sf_params* p) {
+    SF_TRY(need_ctx(ctx));
+    if (!p) return fail(SF_ERR_INVALID_ARGUMENT, "null params");
+    *p = ctx->params;
+    return SF_OK;
+}
+
+SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz, uint32_t n) {
+    SF_TRY(need_ctx(ctx));
+    if (n && !pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null positions");
+    SF_TRY(set_device(ctx));
+    const bool resized = n != ctx->d.n;
+    SF_TRY(alloc_particles(ctx, n));
+    if (resized) drop_graph(ctx);
+    ctx->d.n = n;
+    ctx->sorted = false;
+    if (n == 0) return SF_OK;
+    float* io = ctx->d.io;
+    const size_t bytes = (size_t)n * 3 * sizeof(float);
+    SF_TRY(copy_in(ctx, io, pos_xyz, bytes));
+    if (vel_xyz) {
+        SF_TRY(copy_in(ctx, io + 3 * (size_t)n, vel_xyz, bytes));
+    } else {
+        SF_CUDA(cudaMemsetAsync(io + 3 * (size_t)n, 0, bytes, ctx->stream));
+    }
+    SF_TRY(sort_uploaded(ctx));
+    // The caller may reuse its buffers once this returns.
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint32_t n) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
+    SF_TRY(set_device(ctx));
+    float* io = ctx->d.io;
+    const size_t bytes = (size_t)n * 3 * sizeof(float);
+    sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, pos_xyz ? io : nullptr, vel_xyz ? io + 3 * (size_t)n : nullptr,
+                         ctx->stream);
+    SF_TRY(check_launch("store state"));
+    if (pos_xyz) SF_TRY(copy_out(ctx, pos_xyz, io, bytes));
+    if (vel_xyz) SF_TRY(copy_out(ctx, vel_xyz, io + 3 * (size_t)n, bytes));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out) {
+    SF_TRY(need_ctx(ctx));
+    if (!n_out) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    *n_out = ctx->d.n;
+    return SF_OK;
+}
+
+SF_API sf_status sf_make_ready(sf_ctx* ctx) {
+    SF_TRY(need_sorted(ctx));
+    SF_TRY(set_device(ctx));
+    if (!ctx->step_graph) SF_TRY(capture_step(ctx));
+    return SF_OK;
+}
+
+SF_API sf_status sf_advance_frame(sf_ctx* ctx, float* dt_out) {
+    SF_TRY(sf_step(ctx, 1));
+    if (dt_out) *dt_out = ctx->params.time_step;
+    return SF_OK;
+}
+
+SF_API sf_status sf_step(sf_ctx* ctx, uint32_t nsteps) {
+    SF_TRY(sf_make_ready(ctx));
+    for (uint32_t s = 0; s < nsteps; ++s) SF_CUDA(cudaGraphLaunch(ctx->step_graph, ctx->stream));
+    return SF_OK;
+}
+
+SF_API sf_status sf_synchronize(sf_ctx* ctx) {
+    SF_TRY(need_ctx(ctx));
+    SF_TRY(set_device(ctx));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_stream(sf_ctx* ctx, void** stream_out) {
+    SF_TRY(need_ctx(ctx));
+    if (!stream_out) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    *stream_out = (void*)ctx->stream;
+    return SF_OK;
+}
+
+SF_API sf_status sf_host_alloc(size_t bytes, void** ptr_out) {
+    if (!ptr_out) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    *ptr_out = nullptr;
+    SF_CUDA(cudaMallocHost(ptr_out, bytes ? bytes : 1));
+    return SF_OK;
+}
+
+SF_API sf_status sf_host_free(void* ptr) {
+    if (ptr) SF_CUDA(cudaFreeHost(ptr));
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_grid(const sf_ctx* ctx, uint32_t dims_out[3]) {
+    SF_TRY(need_ctx(ctx));
+    if (!dims_out) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    for (int a = 0; a < 3; ++a) dims_out[a] = (uint32_t)ctx->c.n[a];
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_sorted(sf_ctx* ctx, float* pos4, float* vel4, uint32_t* ids, uint32_t* keys, uint32_t n) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
+    SF_TRY(set_device(ctx));
+    std::vector<float4> p(n);
+    SF_TRY(copy_out(ctx, p.data(), ctx->d.pos, (size_t)n * sizeof(float4)));
+    if (pos4 || ids)
+        for (uint32_t i = 0; i < n; ++i) {
+            uint32_t id;
+            std::memcpy(&id, &p[i].w, sizeof(id));
+            if (ids) ids[i] = id;
+            if (pos4) {
+                pos4[4 * (size_t)i] = p[i].x;
+                pos4[4 * (size_t)i + 1] = p[i].y;
+                pos4[4 * (size_t)i + 2] = p[i].z;
+                pos4[4 * (size_t)i + 3] = 0.f;
+            }
+        }
+    if (vel4) SF_TRY(copy_out(ctx, vel4, ctx->d.vel, (size_t)n * sizeof(float4)));
+    if (keys) {
+        sf::launch_keys(ctx->d.pos, n, ctx->c, ctx->d.tmp, ctx->stream);
+        SF_TRY(check_launch("keys"));
+        SF_TRY(copy_out(ctx, keys, ctx->d.tmp, (size_t)n * sizeof(uint32_t)));
+    }
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_cell_start(sf_ctx* ctx, uint32_t* cell_start, uint32_t count) {
+    SF_TRY(need_sorted(ctx));
+    if (!cell_start || count != ctx->c.ncells + 1)
+        return fail(SF_ERR_INVALID_ARGUMENT, "cell_start needs ncells + 1 entries");
+    SF_TRY(set_device(ctx));
+    return copy_out(ctx, cell_start, ctx->d.cell_start, (size_t)count * sizeof(uint32_t));
+}
+
+SF_API sf_status sf_compute_density(sf_ctx* ctx, float* rho, float* pressure, uint32_t n) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
+    SF_TRY(set_device(ctx));
+    sf::launch_density(ctx->d, ctx->c, ctx->stream);
+    SF_TRY(check_launch("density"));
+    if (rho) SF_TRY(copy_out(ctx, rho, ctx->d.rho, (size_t)n * sizeof(float)));
+    if (pressure) {
+        std::vector<float2> pr(n);
+        SF_TRY(copy_out(ctx, pr.data(), ctx->d.pr, (size_t)n * sizeof(float2)));
+        for (uint32_t i = 0; i < n; ++i) pressure[i] = pr[i].x;
+    }
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+SF_API sf_status sf_compute_accel(sf_ctx* ctx, float* accel_xyz, uint32_t n) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n || !accel_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "bad output or size");
+    SF_TRY(set_device(ctx));
+    if (!ctx->d.accel) SF_CUDA(cudaMalloc(&ctx->d.accel, (size_t)ctx->d.cap * sizeof(float4)));
+    sf::launch_density(ctx->d, ctx->c, ctx->stream);
+    sf::launch_force_only(ctx->d, ctx->c, ctx->stream);
+    SF_TRY(check_launch("forces"));
+    std::vector<float4> a(n);
+    SF_TRY(copy_out(ctx, a.data(), ctx->d.accel, (size_t)n * sizeof(float4)));
+    for (uint32_t i = 0; i < n; ++i) {
+        accel_xyz[3 * (size_t)i] = a[i].x;
+        accel_xyz[3 * (size_t)i + 1] = a[i].y;
+        accel_xyz[3 * (size_t)i + 2] = a[i].z;
+    }
+    return SF_OK;
+}
+
+SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash, uint32_t n) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n || !count || !hash) return fail(SF_ERR_INVALID_ARGUMENT, "bad output or size");
+    SF_TRY(set_device(ctx));
+    // The AoS staging buffer (6 floats per particle) is free between calls.
+    uint32_t* dc = reinterpret_cast<uint32_t*>(ctx->d.io);
+    uint32_t* dh = dc + n;
+    sf::launch_neighbour_stats(ctx->d, ctx->c, dc, dh, ctx->stream);
+    SF_TRY(check_launch("neighbour stats"));
+    SF_TRY(copy_out(ctx, count, dc, (size_t)n * sizeof(uint32_t)));
+    SF_TRY(copy_out(ctx, hash, dh, (size_t)n * sizeof(uint32_t)));
+    return SF_OK;
+}
+
+// ---------------------------------------------------------------- timing
+namespace {
+
+struct EventSet {
+    std::vector<cudaEvent_t> ev;
+    ~EventSet() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    cudaError_t create(size_t n) {
+        ev.assign(n, nullptr);
+        for (size_t i = 0; i < n; ++i) {
+            cudaError_t e = cudaEventCreate(&ev[i]);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+};
+
+struct Scratch {
+    void* p = nullptr;
+    ~Scratch() {
+        if (p) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+SF_API sf_status sf_step_timed(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* total_ms, float* step_ms) {
+    SF_TRY(sf_make_ready(ctx));
+    if (!total_ms) return fail(SF_ERR_INVALID_ARGUMENT, "null total_ms");
+    *total_ms = 0.f;
+    if (!nsteps) return SF_OK;
+    Scratch flush;
+    if (flush_bytes) SF_CUDA(cudaMalloc(&flush.p, flush_bytes));
+    EventSet ev;
+    SF_CUDA(ev.create(2 * (size_t)nsteps));
+    for (uint32_t i = 0; i < nsteps; ++i) {
+        if (flush_bytes) SF_CUDA(cudaMemsetAsync(flush.p, (int)(i & 0xff), flush_bytes, ctx->stream));
+        SF_CUDA(cudaEventRecord(ev.ev[2 * i], ctx->stream));
+        SF_CUDA(cudaGraphLaunch(ctx->step_graph, ctx->stream));
+        SF_CUDA(cudaEventRecord(ev.ev[2 * i + 1], ctx->stream));
+    }
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    double total = 0.0;
+    for (uint32_t i = 0; i < nsteps; ++i) {
+        float ms = 0.f;
+        SF_CUDA(cudaEventElapsedTime(&ms, ev.ev[2 * i], ev.ev[2 * i + 1]));
+        if (step_ms) step_ms[i] = ms;
+        total += ms;
+    }
+    *total_ms = (float)total;
+    return SF_OK;
+}
+
+SF_API uint32_t sf_stage_count(void) { return sf::kNumStages; }
+
+SF_API const char* sf_stage_name(uint32_t stage) { return stage < sf::kNumStages ? sf::kStageNames[stage] : ""; }
+
+SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
+                                  uint32_t nstages) {
+    SF_TRY(need_sorted(ctx));
+    if (!stage_ms || nstages != sf::kNumStages) return fail(SF_ERR_INVALID_ARGUMENT, "stage_ms needs sf_stage_count()");
+    SF_TRY(set_device(ctx));
+    for (uint32_t s = 0; s < nstages; ++s) stage_ms[s] = 0.f;
+    if (!nsteps) return SF_OK;
+    Scratch flush;
+    if (flush_bytes) SF_CUDA(cudaMalloc(&flush.p, flush_bytes));
+    const size_t per = (size_t)sf::kNumStages + 1;
+    EventSet ev;
+    SF_CUDA(ev.create(per * nsteps));
+    for (uint32_t i = 0; i < nsteps; ++i) {
+        if (flush_bytes) SF_CUDA(cudaMemsetAsync(flush.p, (int)(i & 0xff), flush_bytes, ctx->stream));
+        SF_CUDA(cudaEventRecord(ev.ev[per * i], ctx->stream));
+        for (uint32_t s = 0; s < sf::kNumStages; ++s) {
+            sf::enqueue_stage(s, ctx->d, ctx->c, ctx->stream);
+            SF_CUDA(cudaEventRecord(ev.ev[per * i + s + 1], ctx->stream));
+        }
+    }
+    SF_TRY(check_launch("profiled step"));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> acc(sf::kNumStages, 0.0);
+    for (uint32_t i = 0; i < nsteps; ++i)
+        for (uint32_t s = 0; s < sf::kNumStages; ++s) {
+            float ms = 0.f;
+            SF_CUDA(cudaEventElapsedTime(&ms, ev.ev[per * i + s], ev.ev[per * i + s + 1]));
+            acc[s] += ms;
+        }
+    for (uint32_t s = 0; s < sf::kNumStages; ++s) stage_ms[s] = (float)acc[s];
+    return SF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,90 @@
+// sf_internal.h — shared declarations of the GB300 SPH step (not installed).
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/sf_capi.h"
+
+namespace sf {
+
+// Per-step constants, derived once on the host from sf_params (in double,
+// rounded to float) and passed to every kernel by value.
+struct SimConst {
+    float h, h2;          // kernel radius and its square
+    float cd;             // m * 315 / (64 pi h^9): density = cd * sum (h^2 - r^2)^3
+    float cp;             // m * 45 / (pi h^6) / 2: pressure-force coefficient
+    float cv;             // mu * m * 45 / (pi h^6): viscosity-force coefficient
+    float k, rho0, inv_rho0;
+    float dt, e;          // sub-step, boundary restitution
+    float g[3];           // gravity
+    float lo[3], hi[3];   // particle-centre clamp box: box_min + r, box_max - r
+    float bmin[3];        // grid origin
+    float inv_cell[3];    // cells per unit length, per axis
+    int n[3];             // cells per axis
+    int eos, attractive;
+    uint32_t ncells;
+    float mass;
+};
+
+// Fill `c` from `p`; returns SF_OK or an error code (with message in `why`).
+int derive_constants(const sf_params& p, SimConst* c, const char** why);
+
+// Scene generator (sf_scenes.cpp): AoS float3 positions of `scene`.
+int scene_points(const sf_params& p, int scene, uint64_t seed, std::vector<float>& out, const char** why);
+
+// Device buffers of one solver context (all owned by the context).
+struct DeviceState {
+    uint32_t n = 0, cap = 0;
+    float4* pos = nullptr;   // sorted positions, w = original index (bit pattern)
+    float4* vel = nullptr;   // sorted velocities, w = 0
+    float4* pos2 = nullptr;  // integrated positions before the re-sort
+    float4* vel2 = nullptr;
+    float2* pr = nullptr;    // (pressure, 1/density) of the last density pass
+    float* rho = nullptr;    // density of the last density pass
+    uint2* key_slot = nullptr;  // (cell key, arrival slot) of pos2/vel2 order
+    uint32_t* tmp = nullptr;    // cell-bucketed unsorted indices
+    float* io = nullptr;        // AoS staging, 6 floats per particle
+    float4* accel = nullptr;    // optional acceleration output (inspection)
+    // grid
+    uint32_t ncells = 0, ncells_pad = 0;
+    uint32_t* counts = nullptr;      // ncells_pad, zero between steps
+    uint32_t* cell_start = nullptr;  // ncells + 1
+    uint32_t* tile_sums = nullptr;   // one per scan tile
+    uint32_t ntiles = 0;
+};
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// ---- kernel launchers (sf_kernels.cu); all enqueue on `s` ---------------
+void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
+void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s);
+void launch_hash_count(const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts, uint2* key_slot,
+                       cudaStream_t s);
+void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
+void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, cudaStream_t s);
+void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
+                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s);
+void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
+// forces + symplectic Euler + box + next-step cell hash into pos2/vel2
+void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s);
+// forces only: acceleration into d.accel (inspection)
+void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s);
+void launch_keys(const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys, cudaStream_t s);
+void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
+                            cudaStream_t s);
+
+// The sort tail shared by makeReady and every step: counts -> cell_start,
+// bucket, stable rank, gather pos2/vel2 -> pos/vel.
+void enqueue_sort_tail(DeviceState& d, cudaStream_t s);
+// One full sub-step on the sorted state.
+void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);
+
+// The sub-step as separately launchable stages (for per-stage timing).
+constexpr uint32_t kNumStages = 7;
+extern const char* const kStageNames[kNumStages];
+void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s);
+
+}  // namespace sf

@@ -1,0 +1,423 @@
+// sf_kernels.cu — sm_103a kernels of the SPH sub-step.
+//
+// One sub-step (the body of SPHSolver<float>::advanceFrame, called at
+// Source/Simulator.cpp:49 of the reference) on particles kept in cell-sorted
+// order:
+//   k_density          poly6 density + equation of state        (1 thread / particle)
+//   k_force<true>      spiky pressure + viscosity + gravity, symplectic Euler,
+//                      box clamp with restitution, next cell key + arrival slot
+//   k_scan_*           counts -> cell_start (exclusive scan), counts := 0
+//   k_scatter          bucket unsorted indices by cell
+//   k_rank_gather      stable rank inside each cell, gather pos/vel to sorted slots
+// The sort is a one-pass counting (radix-`ncells`) sort: its histogram is the
+// cell table, so cell start/end come out of the same scan.  Stability (equal
+// keys keep their previous order) is restored by ranking each particle among
+// its cell's members, which makes the order deterministic and identical to a
+// stable sort.
+//
+// This translation unit is compiled with -fmad=false: multiply-adds are fused
+// only where fmaf() is written, so the arithmetic matches the CPU oracle
+// operation for operation.
+#include <cuda_runtime.h>
+
+#include "sf_internal.h"
+
+namespace sf {
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ int cell_coord(float x, float bmin, float inv_cell, int n) {
+    const float t = floorf((x - bmin) * inv_cell);
+    return (t >= 0.f) ? ((t < (float)n) ? (int)t : n - 1) : 0;  // NaN -> 0
+}
+
+__device__ __forceinline__ uint32_t cell_key(const SimConst& c, float x, float y, float z) {
+    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
+    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
+    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
+    return ((uint32_t)cz * (uint32_t)c.n[1] + (uint32_t)cy) * (uint32_t)c.n[0] + (uint32_t)cx;
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x85ebca6bu;
+    x ^= x >> 13;
+    x *= 0xc2b2ae35u;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Calls f(j) for the neighbour candidates of a particle at (x, y, z) in the
+// canonical order: dz = -1..1, dy = -1..1, then the contiguous sorted range of
+// the row's cells cx-1..cx+1.
+template <typename F>
+__device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs, float x, float y,
+                                               float z, F&& f) {
+    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
+    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
+    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
+    const int x0 = max(cx - 1, 0), x1 = min(cx + 1, c.n[0] - 1);
+#pragma unroll 1
+    for (int zz = cz - 1; zz <= cz + 1; ++zz) {
+        if (zz < 0 || zz >= c.n[2]) continue;
+#pragma unroll 1
+        for (int yy = cy - 1; yy <= cy + 1; ++yy) {
+            if (yy < 0 || yy >= c.n[1]) continue;
+            const uint32_t row = ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
+            const uint32_t b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
+#pragma unroll 2
+            for (uint32_t j = b; j < e; ++j) f(j);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- state IO
+__global__ void k_load_aos(const float* __restrict__ pos3, const float* __restrict__ vel3, uint32_t n,
+                           float4* __restrict__ pos, float4* __restrict__ vel) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pos[i] = make_float4(pos3[3 * (size_t)i], pos3[3 * (size_t)i + 1], pos3[3 * (size_t)i + 2], __uint_as_float(i));
+    if (vel3)
+        vel[i] = make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.f);
+    else
+        vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_store_aos(const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
+                            float* __restrict__ pos3, float* __restrict__ vel3) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const uint32_t id = __float_as_uint(p.w);
+    if (id >= n) return;  // never for a consistent state
+    if (pos3) {
+        pos3[3 * (size_t)id] = p.x;
+        pos3[3 * (size_t)id + 1] = p.y;
+        pos3[3 * (size_t)id + 2] = p.z;
+    }
+    if (vel3) {
+        const float4 v = vel[i];
+        vel3[3 * (size_t)id] = v.x;
+        vel3[3 * (size_t)id + 1] = v.y;
+        vel3[3 * (size_t)id + 2] = v.z;
+    }
+}
+
+// ---------------------------------------------------------------- hashing
+__global__ void k_hash_count(const float4* __restrict__ pos, uint32_t n, SimConst c, uint32_t* __restrict__ counts,
+                             uint2* __restrict__ key_slot) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const uint32_t key = cell_key(c, p.x, p.y, p.z);
+    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+}
+
+__global__ void k_keys(const float4* __restrict__ pos, uint32_t n, SimConst c, uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    keys[i] = cell_key(c, p.x, p.y, p.z);
+}
+
+// ---------------------------------------------------------------- scan
+__device__ __forceinline__ uint32_t warp_inclusive(uint32_t x) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    return x;
+}
+
+// Exclusive scan over a 1024-thread block; *total receives the block sum.
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_inclusive(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = warp_sums[lane];
+        const uint32_t wi = warp_inclusive(w);
+        warp_sums[lane] = wi - w;
+        if (lane == 31) *total = wi;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + inc - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint4* __restrict__ counts,
+                                                              uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t total;
+    const uint4 q = counts[(size_t)blockIdx.x * kScanThreads + threadIdx.x];
+    block_exclusive(q.x + q.y + q.z + q.w, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(uint32_t* __restrict__ tile_sums, uint32_t ntiles) {
+    __shared__ uint32_t total;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < ntiles; base += kScanThreads) {
+        const uint32_t t = base + threadIdx.x;
+        const uint32_t v = t < ntiles ? tile_sums[t] : 0u;
+        const uint32_t ex = block_exclusive(v, &total);
+        if (t < ntiles) tile_sums[t] = carry + ex;
+        carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint4* __restrict__ counts,
+                                                             const uint32_t* __restrict__ tile_sums,
+                                                             uint4* __restrict__ cell_start) {
+    __shared__ uint32_t total;
+    const size_t t = (size_t)blockIdx.x * kScanThreads + threadIdx.x;
+    const uint4 q = counts[t];
+    const uint32_t ex = block_exclusive(q.x + q.y + q.z + q.w, &total) + tile_sums[blockIdx.x];
+    cell_start[t] = make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
+    counts[t] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// ---------------------------------------------------------------- reorder
+__global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start, uint32_t n,
+                          uint32_t* __restrict__ tmp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 ks = key_slot[i];
+    tmp[cell_start[ks.x] + ks.y] = i;
+}
+
+__global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start,
+                              const uint32_t* __restrict__ tmp, const float4* __restrict__ pos_in,
+                              const float4* __restrict__ vel_in, uint32_t n, float4* __restrict__ pos_out,
+                              float4* __restrict__ vel_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t key = key_slot[i].x;
+    const uint32_t b = cell_start[key], e = cell_start[key + 1];
+    uint32_t rank = 0;
+    for (uint32_t t = b; t < e; ++t) rank += (tmp[t] < i) ? 1u : 0u;
+    const uint32_t dst = b + rank;
+    pos_out[dst] = pos_in[i];
+    vel_out[dst] = vel_in[i];
+}
+
+// ---------------------------------------------------------------- density
+__global__ void __launch_bounds__(kBlock) k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs,
+                                                    uint32_t n, SimConst c, float* __restrict__ rho_out,
+                                                    float2* __restrict__ pr_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = pos[i];
+    float s = 0.f;
+    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
+        const float4 xj = ldg4(pos + j);
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        if (r2 < c.h2) {
+            const float q = c.h2 - r2;
+            s = fmaf(q * q, q, s);
+        }
+    });
+    const float rho = c.cd * s;
+    float p;
+    if (c.eos == SF_EOS_TAIT) {
+        const float x = rho * c.inv_rho0;
+        const float x2 = x * x;
+        const float x4 = x2 * x2;
+        const float x7 = (x4 * x2) * x;
+        p = c.k * (x7 - 1.f);
+    } else {
+        p = c.k * (rho - c.rho0);
+    }
+    if (!c.attractive) p = (p < 0.f) ? 0.f : p;
+    rho_out[i] = rho;
+    pr_out[i] = make_float2(p, 1.f / rho);
+}
+
+// ---------------------------------------------------------------- forces
+template <bool kIntegrate>
+__global__ void __launch_bounds__(kBlock)
+    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
+            const uint32_t* __restrict__ cs, uint32_t n, SimConst c, float4* __restrict__ pos_out,
+            float4* __restrict__ vel_out, uint32_t* __restrict__ counts, uint2* __restrict__ key_slot,
+            float4* __restrict__ acc_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = pos[i];
+    const float4 vi = vel[i];
+    const float2 pri = pr[i];
+    float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
+    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
+        if (j == i) return;
+        const float4 xj = ldg4(pos + j);
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        if (r2 < c.h2) {
+            const float r = sqrtf(r2);
+            const float hr = c.h - r;
+            const float2 prj = __ldg(pr + j);
+            const float4 vj = ldg4(vel + j);
+            const float w = hr * prj.y;
+            avx = fmaf(w, vj.x - vi.x, avx);
+            avy = fmaf(w, vj.y - vi.y, avy);
+            avz = fmaf(w, vj.z - vi.z, avz);
+            if (r > 0.f) {
+                const float sp = ((pri.x + prj.x) * w) * (hr / r);
+                apx = fmaf(sp, dx, apx);
+                apy = fmaf(sp, dy, apy);
+                apz = fmaf(sp, dz, apz);
+            }
+        }
+    });
+    const float ax = fmaf(fmaf(c.cp, apx, c.cv * avx), pri.y, c.g[0]);
+    const float ay = fmaf(fmaf(c.cp, apy, c.cv * avy), pri.y, c.g[1]);
+    const float az = fmaf(fmaf(c.cp, apz, c.cv * avz), pri.y, c.g[2]);
+    if (!kIntegrate) {
+        acc_out[i] = make_float4(ax, ay, az, 0.f);
+        return;
+    }
+    float v[3] = {fmaf(c.dt, ax, vi.x), fmaf(c.dt, ay, vi.y), fmaf(c.dt, az, vi.z)};
+    float x[3] = {fmaf(c.dt, v[0], xi.x), fmaf(c.dt, v[1], xi.y), fmaf(c.dt, v[2], xi.z)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (x[a] < c.lo[a]) {
+            x[a] = c.lo[a];
+            if (v[a] < 0.f) v[a] = -c.e * v[a];
+        }
+        if (x[a] > c.hi[a]) {
+            x[a] = c.hi[a];
+            if (v[a] > 0.f) v[a] = -c.e * v[a];
+        }
+    }
+    pos_out[i] = make_float4(x[0], x[1], x[2], xi.w);
+    vel_out[i] = make_float4(v[0], v[1], v[2], 0.f);
+    const uint32_t key = cell_key(c, x[0], x[1], x[2]);
+    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+}
+
+// ---------------------------------------------------------------- inspection
+__global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n,
+                                  SimConst c, uint32_t* __restrict__ count, uint32_t* __restrict__ hash) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = pos[i];
+    uint32_t cnt = 0, h = 0;
+    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
+        if (j == i) return;
+        const float4 xj = ldg4(pos + j);
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2) {
+            ++cnt;
+            h += mix32(__float_as_uint(xj.w));
+        }
+    });
+    count[i] = cnt;
+    hash[i] = h;
+}
+
+inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s) {
+    if (n) k_load_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, n, pos, vel);
+}
+
+void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s) {
+    if (n) k_store_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, vel, n, pos3, vel3);
+}
+
+void launch_hash_count(const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts, uint2* key_slot,
+                       cudaStream_t s) {
+    if (n) k_hash_count<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, counts, key_slot);
+}
+
+void launch_keys(const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys, cudaStream_t s) {
+    if (n) k_keys<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, keys);
+}
+
+static void launch_scan_reduce(DeviceState& d, cudaStream_t s) {
+    k_scan_reduce<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums);
+}
+static void launch_scan_tiles(DeviceState& d, cudaStream_t s) {
+    k_scan_tiles<<<1, kScanThreads, 0, s>>>(d.tile_sums, d.ntiles);
+}
+static void launch_scan_apply(DeviceState& d, cudaStream_t s) {
+    k_scan_apply<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<uint4*>(d.counts), d.tile_sums,
+                                                   reinterpret_cast<uint4*>(d.cell_start));
+}
+
+void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
+    launch_scan_reduce(d, s);
+    launch_scan_tiles(d, s);
+    launch_scan_apply(d, s);
+}
+
+void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, cudaStream_t s) {
+    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp);
+}
+
+void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
+                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s) {
+    if (n)
+        k_rank_gather<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, tmp, pos_in, vel_in, n, pos_out,
+                                                             vel_out);
+}
+
+void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (d.n) k_density<<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, d.rho, d.pr);
+}
+
+void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (d.n)
+        k_force<true><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.n, c, d.pos2,
+                                                               d.vel2, d.counts, d.key_slot, nullptr);
+}
+
+void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (d.n)
+        k_force<false><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.n, c, nullptr,
+                                                                nullptr, nullptr, nullptr, d.accel);
+}
+
+void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
+                            cudaStream_t s) {
+    if (d.n) k_neighbour_stats<<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, count, hash);
+}
+
+void enqueue_sort_tail(DeviceState& d, cudaStream_t s) {
+    launch_scan_cells(d, d.n, s);
+    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, s);
+    launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
+}
+
+const char* const kStageNames[kNumStages] = {"density",    "force_integrate", "scan_reduce", "scan_tiles",
+                                             "scan_apply", "scatter",         "rank_gather"};
+
+void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s) {
+    switch (stage) {
+        case 0: launch_density(d, c, s); break;
+        case 1: launch_force_integrate(d, c, s); break;
+        case 2: launch_scan_reduce(d, s); break;
+        case 3: launch_scan_tiles(d, s); break;
+        case 4: launch_scan_apply(d, s); break;
+        case 5: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, s); break;
+        case 6: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
+        default: break;
+    }
+}
+
+void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    for (uint32_t st = 0; st < kNumStages; ++st) enqueue_stage(st, d, c, s);
+}
+
+}  // namespace sf

@@ -1,0 +1,373 @@
+"""Python mirror of the reference's solver-facing interface, over the C ABI.
+
+Names, argument meanings and call order follow the reference:
+
+* ``SPHParameters``  — the fields of ``SPHParameters<float>`` that
+  Source/Controller.cpp:54-61 writes, plus ``particleRadius`` and ``scene``
+  (Source/SceneManager.cpp:23,45) and the constants the workloads fix.
+* ``SPHSolver``      — ``SPHSolver<float>`` as used through ``QtSPHSolver``
+  (Include/QtSPHSolver.h:27-35): ``makeReady``, ``advanceFrame``,
+  ``getNumParticles``, ``getParticles``, ``getVelocity``.
+* ``SceneManager``   — Source/SceneManager.cpp:21-173.
+* ``Simulator``      — the headless frame loop of Source/Simulator.cpp:22-103.
+
+All compute runs in the CUDA library; there is no CPU fallback.  Constructing
+an ``SPHSolver`` without a GPU raises ``SFError`` (SF_ERR_NO_DEVICE).
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from ctypes import byref, c_float, c_uint32, c_void_p
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _capi as C
+
+
+def _vp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(c_void_p)
+
+
+@dataclass
+class SPHParameters:
+    """Mirror of ``SPHParameters<float>``; defaults are the 16k dambreak workload."""
+
+    numThreads: int = 0
+    kernelRadius: float = 0.04
+    particleRadius: float = 0.01
+    pressureStiffness: float = 50.0
+    boundaryRestitution: float = 0.1
+    viscosity: float = 0.01
+    stopTime: float = 5.0
+    bUseAttractivePressure: bool = False
+    scene: int = C.SF_SCENE_DAMBREAK_16K
+    restDensity: float = 1000.0
+    gravity: tuple = (0.0, -9.8, 0.0)
+    timeStep: float = 1e-4
+    boxMin: tuple = (0.0, 0.0, 0.0)
+    boxMax: tuple = (1.0, 1.0, 1.0)
+    eos: int = C.SF_EOS_LINEAR
+
+    def to_c(self) -> C.sf_params:
+        p = C.sf_params()
+        p.num_threads = int(self.numThreads)
+        p.kernel_radius = self.kernelRadius
+        p.particle_radius = self.particleRadius
+        p.pressure_stiffness = self.pressureStiffness
+        p.boundary_restitution = self.boundaryRestitution
+        p.viscosity = self.viscosity
+        p.stop_time = self.stopTime
+        p.use_attractive_pressure = 1 if self.bUseAttractivePressure else 0
+        p.scene = int(self.scene)
+        p.rest_density = self.restDensity
+        for a in range(3):
+            p.gravity[a] = self.gravity[a]
+            p.box_min[a] = self.boxMin[a]
+            p.box_max[a] = self.boxMax[a]
+        p.time_step = self.timeStep
+        p.eos = int(self.eos)
+        return p
+
+    @classmethod
+    def from_c(cls, p: C.sf_params) -> "SPHParameters":
+        return cls(numThreads=p.num_threads, kernelRadius=p.kernel_radius, particleRadius=p.particle_radius,
+                   pressureStiffness=p.pressure_stiffness, boundaryRestitution=p.boundary_restitution,
+                   viscosity=p.viscosity, stopTime=p.stop_time, bUseAttractivePressure=bool(p.use_attractive_pressure),
+                   scene=p.scene, restDensity=p.rest_density, gravity=tuple(p.gravity), timeStep=p.time_step,
+                   boxMin=tuple(p.box_min), boxMax=tuple(p.box_max), eos=p.eos)
+
+    def updateParams(self) -> None:
+        """SPHParameters::updateParams() (Source/Controller.cpp:63): validate."""
+        p = self.to_c()
+        C.check(C.load().sf_params_update(byref(p)))
+
+    @classmethod
+    def for_resolution(cls, resolution: int, **kw) -> "SPHParameters":
+        """The GUI's resolution control: kernelRadius = 2 / resolution (Source/Controller.cpp:55)."""
+        return cls(kernelRadius=2.0 / float(resolution), **kw)
+
+
+class SPHSolver:
+    """``SPHSolver<float>`` on one GB300, driven through the C ABI."""
+
+    def __init__(self, params: SPHParameters):
+        self._lib = C.load()
+        self.params = params
+        self._ctx = c_void_p()
+        cp = params.to_c()
+        C.check(self._lib.sf_create(byref(cp), byref(self._ctx)))
+        self._n = 0
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.sf_destroy(self._ctx)
+            self._ctx = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> c_void_p:
+        return self._ctx
+
+    def setParams(self, params: SPHParameters) -> None:
+        cp = params.to_c()
+        C.check(self._lib.sf_set_params(self._ctx, byref(cp)))
+        self.params = params
+
+    # -- state: getParticles()/getVelocity() ------------------------------
+    def setParticles(self, particles: np.ndarray, velocity: Optional[np.ndarray] = None) -> None:
+        pos = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 3)
+        vel = None if velocity is None else np.ascontiguousarray(velocity, dtype=np.float32).reshape(-1, 3)
+        if vel is not None and vel.shape != pos.shape:
+            raise ValueError("velocity must have the same shape as particles")
+        C.check(self._lib.sf_set_state(self._ctx, _vp(pos), _vp(vel), pos.shape[0]))
+        self._n = pos.shape[0]
+
+    def getNumParticles(self) -> int:
+        n = c_uint32()
+        C.check(self._lib.sf_get_num_particles(self._ctx, byref(n)))
+        return n.value
+
+    def getParticles(self) -> np.ndarray:
+        n = self.getNumParticles()
+        out = np.empty((n, 3), np.float32)
+        C.check(self._lib.sf_get_state(self._ctx, _vp(out), None, n))
+        return out
+
+    def getVelocity(self) -> np.ndarray:
+        n = self.getNumParticles()
+        out = np.empty((n, 3), np.float32)
+        C.check(self._lib.sf_get_state(self._ctx, None, _vp(out), n))
+        return out
+
+    def getState(self):
+        n = self.getNumParticles()
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        C.check(self._lib.sf_get_state(self._ctx, _vp(pos), _vp(vel), n))
+        return pos, vel
+
+    # -- stepping ------------------------------------------------------------
+    def makeReady(self) -> None:
+        C.check(self._lib.sf_make_ready(self._ctx))
+
+    def advanceFrame(self) -> float:
+        dt = c_float()
+        C.check(self._lib.sf_advance_frame(self._ctx, byref(dt)))
+        return dt.value
+
+    def step(self, nsteps: int) -> None:
+        C.check(self._lib.sf_step(self._ctx, int(nsteps)))
+
+    def synchronize(self) -> None:
+        C.check(self._lib.sf_synchronize(self._ctx))
+
+    # -- inspection of the cell-sorted internal order ------------------------
+    def gridDims(self) -> tuple:
+        d = (c_uint32 * 3)()
+        C.check(self._lib.sf_get_grid(self._ctx, d))
+        return tuple(d)
+
+    def sortedState(self):
+        n = self.getNumParticles()
+        pos = np.empty((n, 4), np.float32)
+        vel = np.empty((n, 4), np.float32)
+        ids = np.empty(n, np.uint32)
+        keys = np.empty(n, np.uint32)
+        C.check(self._lib.sf_get_sorted(self._ctx, _vp(pos), _vp(vel), _vp(ids), _vp(keys), n))
+        return pos[:, :3].copy(), vel[:, :3].copy(), ids, keys
+
+    def cellStart(self) -> np.ndarray:
+        nx, ny, nz = self.gridDims()
+        out = np.empty(nx * ny * nz + 1, np.uint32)
+        C.check(self._lib.sf_get_cell_start(self._ctx, _vp(out), out.size))
+        return out
+
+    def computeDensity(self):
+        n = self.getNumParticles()
+        rho = np.empty(n, np.float32)
+        prs = np.empty(n, np.float32)
+        C.check(self._lib.sf_compute_density(self._ctx, _vp(rho), _vp(prs), n))
+        return rho, prs
+
+    def computeAccel(self) -> np.ndarray:
+        n = self.getNumParticles()
+        acc = np.empty((n, 3), np.float32)
+        C.check(self._lib.sf_compute_accel(self._ctx, _vp(acc), n))
+        return acc
+
+    def neighbourStats(self):
+        n = self.getNumParticles()
+        cnt = np.empty(n, np.uint32)
+        hsh = np.empty(n, np.uint32)
+        C.check(self._lib.sf_neighbour_stats(self._ctx, _vp(cnt), _vp(hsh), n))
+        return cnt, hsh
+
+
+def scene_positions(params: SPHParameters, scene: int, seed: int = 20171) -> np.ndarray:
+    """Positions of a scene from the library's generator (host code, no GPU needed)."""
+    lib = C.load()
+    cp = params.to_c()
+    n = c_uint32()
+    C.check(lib.sf_scene_count(byref(cp), int(scene), seed, byref(n)))
+    out = np.empty((n.value, 3), np.float32)
+    C.check(lib.sf_setup_scene(byref(cp), int(scene), seed, _vp(out), None, n.value, byref(n)))
+    return out
+
+
+class SceneManager:
+    """Source/SceneManager.cpp:21-173 — fills particle and velocity arrays."""
+
+    def __init__(self, params: SPHParameters, seed: int = 20171):
+        self.params = params
+        self.seed = seed
+
+    def setupScene(self):
+        return self._make(self.params.scene)
+
+    def setupSceneCubeDrop(self):
+        return self._make(C.SF_SCENE_CUBE_DROP)
+
+    def setupSceneSphereDrop(self):
+        return self._make(C.SF_SCENE_SPHERE_DROP)
+
+    def setupSceneDambreak(self):
+        return self._make(C.SF_SCENE_DAMBREAK)
+
+    def setupSceneDoubleDambreak(self):
+        return self._make(C.SF_SCENE_DOUBLE_DAMBREAK)
+
+    def _make(self, scene: int):
+        pos = scene_positions(self.params, scene, self.seed)
+        return pos, np.zeros_like(pos)
+
+
+FRAME_TIME = 0.0333333333  # Source/Simulator.cpp:47
+
+
+def substeps_per_frame(dt: float) -> int:
+    """Sub-steps the frame loop of Source/Simulator.cpp:46-51 takes with a fixed
+    dt: frameTime (float32) accumulates dt until it reaches 1/30 s."""
+    ft = np.float32(0.0)
+    k = 0
+    d = np.float32(dt)
+    while float(ft) < FRAME_TIME:
+        ft = np.float32(ft + d)
+        k += 1
+    return k
+
+
+class Simulator:
+    """Headless restatement of Source/Simulator.cpp:22-103.
+
+    Qt signals become optional callbacks: ``particleChanged`` (per sub-step,
+    Source/Simulator.cpp:50), ``systemTimeChanged`` / ``frameFinished`` (per
+    frame, :54-55), ``simulationFinished`` (:60), ``numParticleChanged`` (:102).
+    With no ``particleChanged`` callback a frame's sub-steps are queued as one
+    ``sf_step`` call (same arithmetic, no per-sub-step host round trip).
+    """
+
+    def __init__(self, params: Optional[SPHParameters] = None, seed: int = 20171):
+        self.m_SimParams = params or SPHParameters()
+        self.m_SPHSolver = SPHSolver(self.m_SimParams)
+        self.m_SceneManager = SceneManager(self.m_SimParams, seed)
+        self.m_SimTime = np.float32(0.0)
+        self.m_bStop = True
+        self._worker: Optional[threading.Thread] = None
+        self._error: Optional[BaseException] = None
+        self.particleChanged: Optional[Callable[[], None]] = None
+        self.systemTimeChanged: Optional[Callable[[float], None]] = None
+        self.frameFinished: Optional[Callable[[], None]] = None
+        self.simulationFinished: Optional[Callable[[], None]] = None
+        self.numParticleChanged: Optional[Callable[[int], None]] = None
+
+    def getSimParams(self) -> SPHParameters:
+        return self.m_SimParams
+
+    def isRunning(self) -> bool:
+        return not self.m_bStop
+
+    def startSimulation(self) -> None:
+        self.m_bStop = False
+        self.wait()
+        self._worker = threading.Thread(target=self._run, daemon=True)
+        self._worker.start()
+
+    def _run(self):
+        try:
+            self.doSimulation()
+        except BaseException as e:  # surfaced by wait()
+            self._error = e
+            self.m_bStop = True
+
+    def wait(self) -> None:
+        if self._worker is not None:
+            self._worker.join()
+            self._worker = None
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise e
+
+    def doSimulation(self) -> None:
+        solver = self.m_SPHSolver
+        solver.makeReady()
+        k = substeps_per_frame(self.m_SimParams.timeStep)
+        dt = np.float32(self.m_SimParams.timeStep)
+        while float(self.m_SimTime) < self.m_SimParams.stopTime and not self.m_bStop:
+            frame_time = np.float32(0.0)
+            if self.particleChanged is None:
+                solver.step(k)
+                for _ in range(k):
+                    frame_time = np.float32(frame_time + dt)
+            else:
+                while float(frame_time) < FRAME_TIME:
+                    frame_time = np.float32(frame_time + np.float32(solver.advanceFrame()))
+                    self.particleChanged()
+            self.m_SimTime = np.float32(self.m_SimTime + frame_time)
+            if self.systemTimeChanged:
+                self.systemTimeChanged(float(self.m_SimTime))
+            if self.frameFinished:
+                self.frameFinished()
+        solver.synchronize()
+        if not self.m_bStop:
+            self.m_bStop = True
+            if self.simulationFinished:
+                self.simulationFinished()
+
+    def stop(self) -> None:
+        self.m_bStop = True
+
+    def reset(self) -> None:
+        self.m_bStop = True
+        self.setupScene()
+
+    def changeScene(self, scene: int) -> None:
+        self.m_SimParams.scene = scene
+        self.setupScene()
+
+    def setupScene(self) -> None:
+        self.m_SimTime = np.float32(0.0)
+        if self.systemTimeChanged:
+            self.systemTimeChanged(0.0)
+        self.wait()
+        pos, vel = self.m_SceneManager.setupScene()
+        self.m_SPHSolver.setParams(self.m_SimParams)
+        self.m_SPHSolver.setParticles(pos, vel)
+        if self.particleChanged:
+            self.particleChanged()
+        if self.numParticleChanged:
+            self.numParticleChanged(self.m_SPHSolver.getNumParticles())

@@ -1,0 +1,94 @@
+"""Generate the golden fixtures in tests/golden/.
+
+1. ``ref_scenes.npz`` — positions written by the reference's OWN scene
+   generator (Source/SceneManager.cpp, compiled in place by oracle/build_ref.sh
+   into oracle/_ref/libref_scenes.so) for the four SimulationScenes at several
+   particle radii.  Small cases are stored whole; all cases carry a SHA-256 of
+   the float32 bytes and the particle count.  These pin the scene generators of
+   the oracle and of the product.
+2. ``oracle_regression.npz`` — outputs of the CPU oracle (built on x86-64) for a
+   small SPH case: one sort, density, acceleration and 5 full steps.  They are a
+   regression record of the oracle itself (not a pin to the reference's solver,
+   which is absent) and let a run on another host architecture check that its
+   oracle build computes the same bits.
+
+Run from the repository root when the reference tree is present:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from simplefluid_gb300._capi import sf_params  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# (scene id, particle radius); radii chosen so counts stay small for whole storage
+REF_CASES = [(s, r) for s in range(4) for r in (0.05, 0.04, 1 / 32, 0.025, 0.02, 1 / 64, 0.01)]
+WHOLE_LIMIT = 20000
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+
+def small_params() -> sf_params:
+    p = sf_params()
+    p.num_threads = 0
+    p.particle_radius = 0.02
+    p.kernel_radius = 0.08
+    p.pressure_stiffness = 50.0
+    p.boundary_restitution = 0.1
+    p.viscosity = 0.01
+    p.stop_time = 5.0
+    p.rest_density = 1000.0
+    p.gravity[1] = -9.8
+    p.time_step = 1e-4
+    for a in range(3):
+        p.box_min[a] = 0.0
+        p.box_max[a] = 1.0
+    return p
+
+
+def main() -> None:
+    O.build(force=True)
+    if O.build_ref() is None:
+        raise SystemExit("reference tree not available: cannot build oracle/_ref")
+    out = {}
+    for s, r in REF_CASES:
+        pos = O.ref_scene(s, r)
+        key = f"s{s}_r{r:.6f}"
+        out[f"{key}_n"] = np.array(pos.shape[0], np.int64)
+        out[f"{key}_sha"] = np.array(sha(pos))
+        out[f"{key}_r"] = np.array(r, np.float32)
+        out[f"{key}_scene"] = np.array(s, np.int32)
+        if pos.shape[0] <= WHOLE_LIMIT:
+            out[f"{key}_pos"] = pos
+    np.savez_compressed(os.path.join(HERE, "ref_scenes.npz"), **out)
+
+    # oracle regression: 10x20x10 block, jitter-free, small box
+    p = small_params()
+    pos = O.scene(p, 16)[:2000]  # first 2000 of the 20x40x20 block (r=0.02 spacing 0.04)
+    st = O.State(pos)
+    keys, cs = st.sort(p, want_cells=True)
+    rho, prs, inv = st.density(p)
+    acc = st.accel(p, prs, inv)
+    cnt, hsh = st.neighbour_stats(p)
+    st2 = O.State(pos)
+    st2.step(p, 5)
+    p5, v5 = st2.original_order()
+    np.savez_compressed(os.path.join(HERE, "oracle_regression.npz"), pos0=pos, keys=keys, ids=st.ids, cell_start=cs,
+                        rho=rho, prs=prs, acc=acc, nbr_count=cnt, nbr_hash=hsh, pos5=p5, vel5=v5)
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

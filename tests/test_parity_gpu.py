@@ -1,0 +1,305 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bars (fixed by the workload definition):
+  * cell keys, sorted order, cell tables and neighbour sets: bit-exact;
+  * single-pass density: within 1e-5 relative per particle (FP32);
+  * single-pass acceleration: within 1e-5 of the field's max magnitude (FP32);
+  * mass (particle count, identity of every particle) conserved exactly;
+  * trajectories: kinetic energy and mean density error over 500 steps within
+    a 1e-3 relative band of the oracle.
+"""
+import numpy as np
+import pytest
+
+from helpers import normwise_err, params_16k, params_1m, params_reference_box, rel_err
+from simplefluid_gb300 import SPHSolver, scene_positions
+from simplefluid_gb300 import _capi as C
+
+pytestmark = pytest.mark.gpu
+
+DENSITY_RTOL = 1e-5
+ACCEL_NORMWISE = 1e-5
+TRAJ_BAND = 1e-3
+
+
+def solver_with(prm, pos, vel=None):
+    s = SPHSolver(prm)
+    s.setParticles(pos, vel)
+    return s
+
+
+def jittered_block(n_side=(16, 24, 16), spacing=0.02, seed=3, origin=0.05):
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(k) for k in n_side], indexing="ij"), -1).reshape(-1, 3)
+    pos = origin + g * spacing + rng.uniform(-0.2, 0.2, size=g.shape) * spacing
+    return pos.astype(np.float32)
+
+
+def test_sort_and_cell_table_bit_exact(oracle):
+    prm = params_16k()
+    pos = scene_positions(prm, C.SF_SCENE_DAMBREAK_16K)
+    rng = np.random.default_rng(0)
+    pos = (pos + rng.uniform(-0.004, 0.004, size=pos.shape)).astype(np.float32)
+    with solver_with(prm, pos) as s:
+        gpos, _, gids, gkeys = s.sortedState()
+        gcs = s.cellStart()
+    st = oracle.State(pos)
+    keys, cs = st.sort(prm.to_c(), want_cells=True)
+    assert np.array_equal(gids, st.ids)
+    assert np.array_equal(gkeys, keys)
+    assert np.array_equal(gcs, cs)
+    assert np.array_equal(gpos.view(np.uint32), st.pos.view(np.uint32))
+
+
+def test_neighbour_sets_bit_exact(oracle):
+    prm = params_16k()
+    pos = jittered_block()
+    with solver_with(prm, pos) as s:
+        gcnt, ghash = s.neighbourStats()
+    st = oracle.State(pos)
+    st.sort(prm.to_c())
+    cnt, hsh = st.neighbour_stats(prm.to_c())
+    assert np.array_equal(gcnt, cnt)
+    assert np.array_equal(ghash, hsh)
+    assert cnt.mean() > 20
+
+
+@pytest.mark.parametrize("eos,attr", [(C.SF_EOS_LINEAR, False), (C.SF_EOS_LINEAR, True), (C.SF_EOS_TAIT, False)])
+def test_density_and_pressure(oracle, eos, attr):
+    prm = params_16k(eos=eos, bUseAttractivePressure=attr)
+    pos = jittered_block()
+    with solver_with(prm, pos) as s:
+        grho, gp = s.computeDensity()
+    st = oracle.State(pos)
+    st.sort(prm.to_c())
+    rho, prs, _ = st.density(prm.to_c())
+    assert rel_err(grho, rho) < DENSITY_RTOL
+    assert normwise_err(gp, prs) < DENSITY_RTOL
+    if not attr:
+        assert np.all(gp >= 0)
+    else:
+        assert np.any(gp < 0)
+
+
+def test_density_op_for_op_equal(oracle):
+    """The kernel performs the oracle's operations in the oracle's order, so the
+    density is not just within tolerance but bit-identical."""
+    prm = params_16k()
+    pos = jittered_block(seed=11)
+    with solver_with(prm, pos) as s:
+        grho, _ = s.computeDensity()
+    st = oracle.State(pos)
+    st.sort(prm.to_c())
+    rho, _, _ = st.density(prm.to_c())
+    assert np.array_equal(grho.view(np.uint32), rho.view(np.uint32))
+
+
+def test_acceleration(oracle):
+    prm = params_16k()
+    pos = jittered_block(seed=5)
+    vel = np.random.default_rng(5).normal(scale=0.3, size=pos.shape).astype(np.float32)
+    with solver_with(prm, pos, vel) as s:
+        gacc = s.computeAccel()
+    st = oracle.State(pos, vel)
+    st.sort(prm.to_c())
+    acc = st.accel(prm.to_c())
+    assert normwise_err(gacc, acc) < ACCEL_NORMWISE
+
+
+def test_one_step_state(oracle):
+    prm = params_16k()
+    pos = jittered_block(seed=9)
+    with solver_with(prm, pos) as s:
+        dt = s.advanceFrame()
+        gpos, gvel = s.getState()
+    assert dt == np.float32(1e-4)
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 1)
+    opos, ovel = st.original_order()
+    assert np.max(np.abs(gpos - opos)) <= 1e-6
+    assert normwise_err(gvel, ovel) < 1e-5
+
+
+def _ke_and_density_error(pos, vel, prm, oracle):
+    ke = 0.5 * float(np.sum(vel.astype(np.float64) ** 2))
+    st = oracle.State(pos, vel)
+    st.sort(prm.to_c())
+    rho, _, _ = st.density(prm.to_c())
+    return ke, float(np.mean(np.abs(rho - prm.restDensity)) / prm.restDensity)
+
+
+def test_trajectory_500_steps_16k(oracle):
+    """500 steps of the 16,000-particle dambreak: kinetic energy and mean density
+    error track the oracle within the stated band; mass is conserved exactly."""
+    prm = params_16k()
+    pos = scene_positions(prm, C.SF_SCENE_DAMBREAK_16K)
+    st = oracle.State(pos)
+    with solver_with(prm, pos) as s:
+        for chunk in range(5):
+            s.step(100)
+            st.step(prm.to_c(), 100)
+            gpos, gvel = s.getState()
+            opos, ovel = st.original_order()
+            gke, gde = _ke_and_density_error(gpos, gvel, prm, oracle)
+            oke, ode = _ke_and_density_error(opos, ovel, prm, oracle)
+            assert abs(gke - oke) <= TRAJ_BAND * max(oke, 1e-12), (chunk, gke, oke)
+            assert abs(gde - ode) <= TRAJ_BAND * max(ode, 1e-12) + 1e-7, (chunk, gde, ode)
+        _, _, ids, keys = s.sortedState()
+        assert s.getNumParticles() == 16000
+        assert np.array_equal(np.sort(ids), np.arange(16000, dtype=np.uint32))
+        assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+        lo = np.float32(0.01)
+        assert np.all(gpos >= lo) and np.all(gpos <= np.float32(0.99))
+        assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
+
+
+@pytest.mark.parametrize("scene", [C.SF_SCENE_SPHERE_DROP, C.SF_SCENE_CUBE_DROP, C.SF_SCENE_DAMBREAK,
+                                   C.SF_SCENE_DOUBLE_DAMBREAK])
+def test_reference_scenes_20_steps(oracle, scene):
+    """The reference's four scenes in its [-1,1]^3 box at GUI resolution 24."""
+    prm = params_reference_box(resolution=24, scene=scene)
+    pos = scene_positions(prm, scene)
+    with solver_with(prm, pos) as s:
+        s.step(20)
+        gpos, gvel = s.getState()
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 20)
+    opos, ovel = st.original_order()
+    assert np.max(np.abs(gpos - opos)) <= 1e-5
+    assert normwise_err(gvel, ovel) < 1e-4
+
+
+def test_set_get_roundtrip_bits():
+    prm = params_16k()
+    pos = jittered_block(seed=2)
+    vel = np.random.default_rng(2).normal(size=pos.shape).astype(np.float32)
+    with solver_with(prm, pos, vel) as s:
+        gpos, gvel = s.getState()
+        assert s.getNumParticles() == pos.shape[0]
+    assert np.array_equal(gpos.view(np.uint32), pos.view(np.uint32))
+    assert np.array_equal(gvel.view(np.uint32), vel.view(np.uint32))
+
+
+def test_deterministic_repeat():
+    prm = params_16k()
+    pos = scene_positions(prm, C.SF_SCENE_DAMBREAK_16K)
+    outs = []
+    for _ in range(2):
+        with solver_with(prm, pos) as s:
+            s.step(50)
+            outs.append(s.getState()[0])
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
+def test_edge_single_particle(oracle):
+    prm = params_16k()
+    pos = np.array([[0.5, 0.5, 0.5]], np.float32)
+    with solver_with(prm, pos) as s:
+        rho, _ = s.computeDensity()
+        s.step(10)
+        gpos, gvel = s.getState()
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 10)
+    assert rho[0] > 0
+    assert np.array_equal(gpos.view(np.uint32), st.pos.view(np.uint32))
+
+
+def test_edge_dense_cluster_one_cell(oracle):
+    """Hundreds of particles in one cell (and coincident pairs): the per-cell
+    ranking and the r = 0 pressure guard."""
+    prm = params_16k()
+    rng = np.random.default_rng(4)
+    pos = (0.5 + rng.uniform(0, 0.03, size=(600, 3))).astype(np.float32)
+    pos[300:310] = pos[0]
+    with solver_with(prm, pos) as s:
+        _, _, ids, keys = s.sortedState()
+        s.step(3)
+        gpos, gvel = s.getState()
+    st = oracle.State(pos)
+    okeys, _ = st.sort(prm.to_c())
+    assert np.array_equal(ids, st.ids) and np.array_equal(keys, okeys)
+    st2 = oracle.State(pos)
+    st2.step(prm.to_c(), 3)
+    opos, ovel = st2.original_order()
+    assert np.isfinite(gpos).all()
+    assert normwise_err(gpos, opos) < 1e-5
+
+
+def test_edge_particles_outside_box(oracle):
+    """Particles given outside the box are binned into the edge cells and
+    clamped back by the first step."""
+    prm = params_16k()
+    pos = jittered_block(n_side=(6, 6, 6))
+    pos[:10] -= 0.5
+    pos[10:20] += 2.0
+    with solver_with(prm, pos) as s:
+        s.step(1)
+        gpos, _ = s.getState()
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 1)
+    opos, _ = st.original_order()
+    assert np.all(gpos >= np.float32(0.01)) and np.all(gpos <= np.float32(0.99))
+    assert np.max(np.abs(gpos - opos)) <= 1e-6
+
+
+def test_errors_through_the_abi(lib):
+    import ctypes
+    prm = params_16k()
+    s = SPHSolver(prm)
+    with pytest.raises(C.SFError) as e:
+        s.advanceFrame()
+    assert e.value.status == C.SF_ERR_NOT_READY
+    s.setParticles(jittered_block(n_side=(4, 4, 4)))
+    out = np.zeros((3, 3), np.float32)
+    st = lib.sf_get_state(s.handle, out.ctypes.data_as(ctypes.c_void_p), None, 3)
+    assert st == C.SF_ERR_INVALID_ARGUMENT
+    s.setParticles(np.zeros((0, 3), np.float32))
+    assert s.getNumParticles() == 0
+    with pytest.raises(C.SFError):
+        s.makeReady()
+    s.close()
+
+
+def test_set_params_regrids(oracle):
+    """Changing kernelRadius re-buckets the particles on the new grid."""
+    prm = params_16k()
+    pos = jittered_block(seed=6)
+    with solver_with(prm, pos) as s:
+        prm2 = params_16k(kernelRadius=0.05)
+        s.setParams(prm2)
+        assert s.gridDims() == (20, 20, 20)
+        gcnt, ghash = s.neighbourStats()
+    st = oracle.State(pos)
+    st.sort(prm2.to_c())
+    cnt, hsh = st.neighbour_stats(prm2.to_c())
+    assert np.array_equal(gcnt, cnt) and np.array_equal(ghash, hsh)
+
+
+def test_full_size_1m_double_dambreak(oracle):
+    """The 1,048,576-particle double dambreak: sort/cell table bit-exact and
+    density within tolerance at full size; after 20 steps the size-independent
+    properties hold (sorted keys, permutation of ids, cell table consistent
+    with the keys, particles inside the box, finite state)."""
+    prm = params_1m()
+    pos = scene_positions(prm, C.SF_SCENE_DOUBLE_DAMBREAK_1M)
+    n = pos.shape[0]
+    assert n == 1048576
+    st = oracle.State(pos)
+    okeys, ocs = st.sort(prm.to_c(), want_cells=True)
+    orho, _, _ = st.density(prm.to_c())
+    with solver_with(prm, pos) as s:
+        _, _, ids, keys = s.sortedState()
+        assert np.array_equal(ids, st.ids) and np.array_equal(keys, okeys)
+        assert np.array_equal(s.cellStart(), ocs)
+        grho, _ = s.computeDensity()
+        assert rel_err(grho, orho) < DENSITY_RTOL
+        s.step(20)
+        _, _, ids, keys = s.sortedState()
+        cs = s.cellStart()
+        gpos, gvel = s.getState()
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+    assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
+    counts = np.bincount(keys, minlength=cs.size - 1)
+    assert cs[0] == 0 and cs[-1] == n and np.array_equal(np.diff(cs.astype(np.int64)), counts)
+    assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
+    assert np.all(gpos >= np.float32(0.0025)) and np.all(gpos <= np.float32(0.9975))
