@@ -153,6 +153,25 @@ def test_trajectory_500_steps_16k(oracle):
         assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
 
 
+def test_trajectory_bit_identical_200_steps(oracle):
+    """Every kernel performs the oracle's floating-point operations in the
+    oracle's order (explicit fmaf, IEEE sqrt and division, canonical neighbour
+    order), so 200 sub-steps of the 16k dambreak agree bit for bit."""
+    prm = params_16k()
+    pos = scene_positions(prm, C.SF_SCENE_DAMBREAK_16K)
+    with solver_with(prm, pos) as s:
+        s.step(200)
+        gpos, gvel = s.getState()
+        _, _, ids, _ = s.sortedState()
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 200)
+    st.sort(prm.to_c())  # the solver leaves its state sorted after each step
+    opos, ovel = st.original_order()
+    assert np.array_equal(ids, st.ids)
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32))
+
+
 @pytest.mark.parametrize("scene", [C.SF_SCENE_SPHERE_DROP, C.SF_SCENE_CUBE_DROP, C.SF_SCENE_DAMBREAK,
                                    C.SF_SCENE_DOUBLE_DAMBREAK])
 def test_reference_scenes_20_steps(oracle, scene):
@@ -267,10 +286,15 @@ def test_set_params_regrids(oracle):
     with solver_with(prm, pos) as s:
         prm2 = params_16k(kernelRadius=0.05)
         s.setParams(prm2)
-        assert s.gridDims() == (20, 20, 20)
+        d = oracle.derive(prm2.to_c())
+        assert s.gridDims() == (int(d["nx"]), int(d["ny"]), int(d["nz"])) == (19, 19, 19)
         gcnt, ghash = s.neighbourStats()
+        _, _, gids, _ = s.sortedState()
+    # the solver re-sorts its current (old-grid) order stably on the new grid
     st = oracle.State(pos)
+    st.sort(prm.to_c())
     st.sort(prm2.to_c())
+    assert np.array_equal(gids, st.ids)
     cnt, hsh = st.neighbour_stats(prm2.to_c())
     assert np.array_equal(gcnt, cnt) and np.array_equal(ghash, hsh)
 
