@@ -186,6 +186,24 @@ SF_API const char* sf_stage_name(uint32_t stage);
 SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
                                   uint32_t nstages);
 
+/* ---- allocation-free density ----------------------------------------------
+ * No counterpart in the reference: an addition of this library for callers
+ * that cannot allocate device memory (an application or plugin that owns a
+ * fixed device-memory budget, a real-time loop where an allocation may block
+ * or fail).  Computes rho and p (equation of state of `p`) of n particles whose
+ * AoS float3 positions are in device memory, writing device outputs in the
+ * caller's particle order; either output may be NULL, not both.  Work is
+ * queued on `stream` (a cudaStream_t; NULL = default stream) and not waited
+ * for.  Calls no allocator: the grid sort runs in one fixed static device
+ * array (about 7.6 MB, held by every GPU that loads the library until exit),
+ * which limits a call to 65,536 particles and 262,144 grid cells; larger
+ * requests fail with SF_ERR_CAPACITY before any GPU work.  All calls share that
+ * array: calls whose GPU work overlaps race, so serialise them on one stream.
+ * The first call on a device looks up the array's address; make it before any
+ * stream capture. */
+SF_API sf_status sf_density_noalloc(const sf_params* p, const float* d_pos_xyz, uint32_t n, float* d_rho,
+                                    float* d_pressure, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,7 @@ PROTOTYPES = {
     "sf_stage_count": (c_uint32, []),
     "sf_stage_name": (c_char_p, [c_uint32]),
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
+    "sf_density_noalloc": (c_int32, [_P(sf_params), c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -29,6 +29,7 @@ SOURCES = [
     ("sf_kernels.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
     ("sf_scenes.cpp", []),
+    ("sf_noalloc.cu", ["-fmad=false"]),
 ]
 
 

@@ -727,4 +727,21 @@ SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_b
     return SF_OK;
 }
 
+// Allocation-free density for callers that cannot allocate device memory;
+// the sort scratch is a fixed static device array (sf_noalloc.cu).
+SF_API sf_status sf_density_noalloc(const sf_params* p, const float* d_pos_xyz, uint32_t n, float* d_rho,
+                                    float* d_pressure, void* stream) {
+    if (!p) return fail(SF_ERR_INVALID_ARGUMENT, "null params");
+    if (n && !d_pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null positions");
+    if (n && !d_rho && !d_pressure) return fail(SF_ERR_INVALID_ARGUMENT, "no output");
+    SF_TRY(validate(*p));
+    sf::SimConst c;
+    const char* why = "";
+    int st = sf::derive_constants(*p, &c, &why);
+    if (st) return fail(st, why);
+    st = sf::noalloc_density(*p, c, d_pos_xyz, n, d_rho, d_pressure, static_cast<cudaStream_t>(stream), &why);
+    if (st) return fail(st, why);
+    return SF_OK;
+}
+
 }  // extern "C"

@@ -87,4 +87,9 @@ constexpr uint32_t kNumStages = 7;
 extern const char* const kStageNames[kNumStages];
 void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s);
 
+// Density of caller-owned device positions using the library's fixed static
+// scratch (sf_noalloc.cu); no device allocation.
+int noalloc_density(const sf_params& p, const SimConst& c, const float* d_pos_xyz, uint32_t n, float* d_rho,
+                    float* d_pressure, cudaStream_t stream, const char** why);
+
 }  // namespace sf
