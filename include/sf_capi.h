@@ -87,7 +87,12 @@ typedef struct sf_params {
     float box_min[3];                /* simulation box                              */
     float box_max[3];
     int32_t eos;                     /* SF_EOS_*                                    */
-    int32_t reserved[3];             /* must be zero                                */
+    int32_t cells_per_h;             /* uniform-grid cells per kernel radius: 1, 2
+                                        or 3 (0 = 2).  The neighbour search visits
+                                        the (2K+1)^3 cells around a particle's cell
+                                        and the summation order follows the grid,
+                                        so K is part of the arithmetic.            */
+    int32_t reserved[2];             /* must be zero                                */
 } sf_params;
 
 typedef struct sf_ctx sf_ctx;
@@ -167,6 +172,23 @@ SF_API sf_status sf_compute_accel(sf_ctx* ctx, float* accel_xyz, uint32_t n);
 /* Per sorted particle: number of neighbours j != i with |xi-xj|^2 < h^2 and a
  * order-independent hash of their original indices. */
 SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash, uint32_t n);
+
+/* ---- kernel tuning -----------------------------------------------------------
+ * Implementation choices of a context's step.  Every choice computes the same
+ * bits; they differ only in speed.  Not part of the reference interface. */
+#define SF_LIST_NONE 0        /* force pass rescans the candidate cells       */
+#define SF_LIST_TILE_STAGED 1 /* density pass stages neighbour lists in shared
+                                 memory, writes 128-particle tiles             */
+#define SF_LIST_TILE 2        /* direct stores, 128-particle tiles             */
+typedef struct sf_tuning {
+    int32_t list_mode;     /* SF_LIST_*                                       */
+    int32_t density_block; /* threads per block of the density pass: 128, 256 */
+    int32_t force_block;   /* threads per block of the force pass: 128, 256   */
+    int32_t prefetch;      /* neighbours gathered per batch: 2 or 4           */
+    int32_t reserved[4];   /* must be zero                                    */
+} sf_tuning;
+SF_API sf_status sf_get_tuning(const sf_ctx* ctx, sf_tuning* t);
+SF_API sf_status sf_set_tuning(sf_ctx* ctx, const sf_tuning* t);
 
 /* ---- measurement ----------------------------------------------------------
  * Device-side timing with CUDA events on the context's stream.  Not part of

@@ -24,12 +24,15 @@
 //
 // Canonical semantics shared with the CUDA path (both sides implement them
 // independently; every choice is fixed here):
-//  * uniform grid over [box_min, box_max] with n_a = max(1, floor(ext_a / h))
-//    cells per axis (cell edge >= h); cell coord = floor((x - box_min) *
-//    inv_cell) clamped to [0, n_a - 1] (NaN -> 0); key = (cz*ny + cy)*nx + cx.
+//  * uniform grid over [box_min, box_max] with K = cells_per_h (0 -> 2) and
+//    n_a = max(1, floor(K * ext_a / h)) cells per axis (cell edge >= h/K);
+//    cell coord = floor((x - box_min) * inv_cell) clamped to [0, n_a - 1]
+//    (NaN -> 0); key = (cz*ny + cy)*nx + cx.
 //  * stable sort of the current particle order by key (counting sort).
-//  * neighbours of sorted particle i are visited in the order dz = -1..1,
-//    dy = -1..1, then the contiguous sorted range of cells cx-1..cx+1.
+//  * neighbours of sorted particle i are visited in the order dz = -K..K,
+//    dy = -K..K, then the contiguous sorted range of cells cx-K..cx+K
+//    (clamped to the grid).  A faster implementation may skip cells that
+//    provably hold no particle within h; that changes no sum.
 //  * explicit fused multiply-adds where written (std::fma), no other
 //    contraction (built with -ffp-contract=off), IEEE sqrt and division.
 //  * derived constants computed in double, then rounded to the working type.
@@ -52,7 +55,7 @@ struct Derived {
     Real h, h2, mass, cd, cp, cv, k, rho0, inv_rho0, dt, e, r;
     Real g[3], lo[3], hi[3], bmin[3], inv_cell[3];
     int n[3];
-    int eos, attractive;
+    int eos, attractive, reach;
     uint64_t ncells;
 };
 
@@ -78,6 +81,9 @@ int derive(const sf_params* p, Derived<Real>* d) {
     d->r = (Real)r;
     d->eos = p->eos;
     d->attractive = p->use_attractive_pressure;
+    const int K = p->cells_per_h ? p->cells_per_h : 2;
+    if (K < 1 || K > 3) return SF_ERR_INVALID_ARGUMENT;
+    d->reach = K;
     d->ncells = 1;
     for (int a = 0; a < 3; ++a) {
         const double ext = (double)p->box_max[a] - (double)p->box_min[a];
@@ -86,14 +92,14 @@ int derive(const sf_params* p, Derived<Real>* d) {
         d->lo[a] = (Real)((double)p->box_min[a] + r);
         d->hi[a] = (Real)((double)p->box_max[a] - r);
         d->bmin[a] = (Real)p->box_min[a];
-        double na = std::floor(ext / h);
+        double na = std::floor((double)K * ext / h);
         if (na < 1) na = 1;
         if (na > 65535) return SF_ERR_GRID_TOO_LARGE;
         d->n[a] = (int)na;
         d->inv_cell[a] = (Real)(na / ext);
         d->ncells *= (uint64_t)d->n[a];
     }
-    if (d->ncells > (1ull << 30)) return SF_ERR_GRID_TOO_LARGE;
+    if (d->ncells > (1ull << 28)) return SF_ERR_GRID_TOO_LARGE;
     return SF_OK;
 }
 
@@ -182,10 +188,11 @@ inline void for_candidates(const Derived<Real>& d, const std::vector<uint32_t>& 
     const int cx = cell_coord(xi[0], d.bmin[0], d.inv_cell[0], d.n[0]);
     const int cy = cell_coord(xi[1], d.bmin[1], d.inv_cell[1], d.n[1]);
     const int cz = cell_coord(xi[2], d.bmin[2], d.inv_cell[2], d.n[2]);
-    const int x0 = std::max(cx - 1, 0), x1 = std::min(cx + 1, d.n[0] - 1);
-    for (int z = cz - 1; z <= cz + 1; ++z) {
+    const int R = d.reach;
+    const int x0 = std::max(cx - R, 0), x1 = std::min(cx + R, d.n[0] - 1);
+    for (int z = cz - R; z <= cz + R; ++z) {
         if (z < 0 || z >= d.n[2]) continue;
-        for (int y = cy - 1; y <= cy + 1; ++y) {
+        for (int y = cy - R; y <= cy + R; ++y) {
             if (y < 0 || y >= d.n[1]) continue;
             const uint64_t row = ((uint64_t)z * d.n[1] + y) * d.n[0];
             const uint32_t b = cs[row + x0], e = cs[row + x1 + 1];

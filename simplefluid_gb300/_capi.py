@@ -54,8 +54,21 @@ class sf_params(ctypes.Structure):
         ("box_min", c_float * 3),
         ("box_max", c_float * 3),
         ("eos", c_int32),
-        ("reserved", c_int32 * 3),
+        ("cells_per_h", c_int32),
+        ("reserved", c_int32 * 2),
     ]
+
+
+SF_LIST_NONE = 0
+SF_LIST_TILE_STAGED = 1
+SF_LIST_TILE = 2
+
+
+class sf_tuning(ctypes.Structure):
+    """Mirror of ``struct sf_tuning`` (include/sf_capi.h)."""
+
+    _fields_ = [("list_mode", c_int32), ("density_block", c_int32), ("force_block", c_int32),
+                ("prefetch", c_int32), ("reserved", c_int32 * 4)]
 
 
 class SFError(RuntimeError):
@@ -100,6 +113,8 @@ PROTOTYPES = {
     "sf_stage_count": (c_uint32, []),
     "sf_stage_name": (c_char_p, [c_uint32]),
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
+    "sf_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_density_noalloc": (c_int32, [_P(sf_params), c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
 }
 

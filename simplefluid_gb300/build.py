@@ -26,7 +26,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 
 # (source, extra flags)
 SOURCES = [
-    ("sf_kernels.cu", ["-fmad=false"]),
+    ("sf_grid.cu", ["-fmad=false"]),
+    ("sf_density.cu", ["-fmad=false"]),
+    ("sf_force.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),

@@ -76,8 +76,9 @@ sf_status validate(const sf_params& p) {
     if (!finite(p.stop_time) || p.stop_time < 0.f) return fail(SF_ERR_INVALID_ARGUMENT, "stop_time must be >= 0");
     if (p.eos != SF_EOS_LINEAR && p.eos != SF_EOS_TAIT) return fail(SF_ERR_INVALID_ARGUMENT, "unknown eos");
     if (p.num_threads < 0) return fail(SF_ERR_INVALID_ARGUMENT, "num_threads must be >= 0");
-    if (p.reserved[0] || p.reserved[1] || p.reserved[2])
-        return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    if (p.cells_per_h < 0 || p.cells_per_h > 3)
+        return fail(SF_ERR_INVALID_ARGUMENT, "cells_per_h must be 1, 2 or 3 (0 = 2)");
+    if (p.reserved[0] || p.reserved[1]) return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
     for (int a = 0; a < 3; ++a) {
         if (!finite(p.gravity[a]) || !finite(p.box_min[a]) || !finite(p.box_max[a]))
             return fail(SF_ERR_INVALID_ARGUMENT, "gravity and box must be finite");
@@ -107,7 +108,7 @@ bool is_pinned(const void* p) {
 }
 
 void free_particles(sf::DeviceState& d) {
-    void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel};
+    void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel, d.nbr, d.nbr_count};
     for (void* b : bufs)
         if (b) cudaFree(b);
     d.pos = d.vel = d.pos2 = d.vel2 = d.accel = nullptr;
@@ -116,6 +117,8 @@ void free_particles(sf::DeviceState& d) {
     d.key_slot = nullptr;
     d.tmp = nullptr;
     d.io = nullptr;
+    d.nbr = nullptr;
+    d.nbr_count = nullptr;
     d.cap = 0;
 }
 
@@ -162,6 +165,9 @@ sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     SF_CUDA(cudaMalloc(&d.key_slot, c * sizeof(uint2)));
     SF_CUDA(cudaMalloc(&d.tmp, c * sizeof(uint32_t)));
     SF_CUDA(cudaMalloc(&d.io, c * 6 * sizeof(float)));
+    const size_t tiles = (c + sf::kNbTile - 1) / sf::kNbTile;
+    SF_CUDA(cudaMalloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t)));
+    SF_CUDA(cudaMalloc(&d.nbr_count, c * sizeof(uint32_t)));
     d.cap = (uint32_t)c;
     return SF_OK;
 }
@@ -265,6 +271,9 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why) {
     c->e = p.boundary_restitution;
     c->eos = p.eos;
     c->attractive = p.use_attractive_pressure ? 1 : 0;
+    const int K = p.cells_per_h ? p.cells_per_h : 2;
+    c->reach = K;
+    double coord_max = 0.0;
     uint64_t cells = 1;
     for (int a = 0; a < 3; ++a) {
         const double ext = (double)p.box_max[a] - (double)p.box_min[a];
@@ -272,7 +281,7 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why) {
         c->lo[a] = (float)((double)p.box_min[a] + r);
         c->hi[a] = (float)((double)p.box_max[a] - r);
         c->bmin[a] = p.box_min[a];
-        double na = std::floor(ext / h);
+        double na = std::floor((double)K * ext / h);
         if (na < 1) na = 1;
         if (na > 65535) {
             *why = "more than 65535 cells along one axis (box / kernel_radius too large)";
@@ -280,8 +289,15 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why) {
         }
         c->n[a] = (int)na;
         c->inv_cell[a] = (float)(na / ext);
+        c->cell_w[a] = (float)(ext / na);
         cells *= (uint64_t)c->n[a];
+        coord_max = std::fmax(coord_max, std::fmax(std::fabs((double)p.box_min[a]), std::fabs((double)p.box_max[a])));
     }
+    // Slack of the pruning bound: a few float ulps of the largest coordinate
+    // (cell assignment and the in-cell offset are each good to ~1 ulp) plus
+    // 1e-5 h.
+    c->prune_margin = (float)(16.0 * std::ldexp(std::fmax(coord_max, 1.0), -23) + 1e-5 * h);
+    c->prune_h2 = (float)(h * h * (1.0 + 1e-4));
     if (cells > kMaxCells) {
         *why = "uniform grid would exceed 2^28 cells (box / kernel_radius too large)";
         return SF_ERR_GRID_TOO_LARGE;
@@ -321,6 +337,7 @@ SF_API sf_status sf_params_default(sf_params* p) {
         p->box_max[a] = 1.0f;
     }
     p->eos = SF_EOS_LINEAR;
+    p->cells_per_h = 2;
     return SF_OK;
 }
 
@@ -687,6 +704,37 @@ SF_API sf_status sf_step_timed(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_byte
         total += ms;
     }
     *total_ms = (float)total;
+    return SF_OK;
+}
+
+SF_API sf_status sf_get_tuning(const sf_ctx* ctx, sf_tuning* t) {
+    SF_TRY(need_ctx(ctx));
+    if (!t) return fail(SF_ERR_INVALID_ARGUMENT, "null tuning");
+    std::memset(t, 0, sizeof(*t));
+    t->list_mode = ctx->d.tune.list_mode;
+    t->density_block = ctx->d.tune.density_block;
+    t->force_block = ctx->d.tune.force_block;
+    t->prefetch = ctx->d.tune.prefetch;
+    return SF_OK;
+}
+
+SF_API sf_status sf_set_tuning(sf_ctx* ctx, const sf_tuning* t) {
+    SF_TRY(need_ctx(ctx));
+    if (!t) return fail(SF_ERR_INVALID_ARGUMENT, "null tuning");
+    if (t->list_mode < SF_LIST_NONE || t->list_mode > SF_LIST_TILE)
+        return fail(SF_ERR_INVALID_ARGUMENT, "unknown list_mode");
+    if ((t->density_block != 128 && t->density_block != 256) || (t->force_block != 128 && t->force_block != 256))
+        return fail(SF_ERR_INVALID_ARGUMENT, "block sizes must be 128 or 256");
+    if (t->prefetch != 2 && t->prefetch != 4) return fail(SF_ERR_INVALID_ARGUMENT, "prefetch must be 2 or 4");
+    if (t->reserved[0] || t->reserved[1] || t->reserved[2] || t->reserved[3])
+        return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    SF_TRY(set_device(ctx));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->d.tune.list_mode = t->list_mode;
+    ctx->d.tune.density_block = t->density_block;
+    ctx->d.tune.force_block = t->force_block;
+    ctx->d.tune.prefetch = t->prefetch;
+    drop_graph(ctx);
     return SF_OK;
 }
 

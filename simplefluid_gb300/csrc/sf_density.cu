@@ -1,0 +1,80 @@
+// sf_density.cu — density pass of the SPH sub-step (sm_103a).
+//
+// One thread per cell-sorted particle.  Poly6 density over the canonical
+// candidates; non-neighbours add an exact zero (fma(0, 0, s) == s), so the sum
+// is branch-free and bit-identical to summing neighbours only.  The pass also
+// evaluates the equation of state and records each particle's j != i
+// neighbours, in canonical order, for the force pass:
+//   kEmitNone    no list (the force pass rescans the candidate cells);
+//   kEmitStaged  list staged in shared memory, written out in full lines;
+//   kEmitTile    list written directly.
+// Both list modes use the tile layout of nbr_index().  nbr_count[i] is the
+// full count; a count above kNbCap makes the force pass rescan that particle's
+// candidates instead of reading the list.
+#include "sf_device.cuh"
+
+namespace sf {
+namespace {
+
+template <int kMode, int kBlockSize, int kReach>
+__global__ void __launch_bounds__(kBlockSize)
+    k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n, SimConst c,
+              float* __restrict__ rho_out, float2* __restrict__ pr_out, uint32_t* __restrict__ nbr,
+              uint32_t* __restrict__ nbr_count) {
+    __shared__ uint32_t s_nb[kMode == kEmitStaged ? kNbCap : 1][kMode == kEmitStaged ? kBlockSize : 1];
+    const uint32_t t = threadIdx.x;
+    const uint32_t i = blockIdx.x * kBlockSize + t;
+    uint32_t cnt = 0;
+    if (i < n) {
+        const float4 xi = pos[i];
+        float s = 0.f;
+        for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const bool near = r2 < c.h2;
+            const float q = near ? c.h2 - r2 : 0.f;
+            s = fmaf(q * q, q, s);
+            if (kMode != kEmitNone && near && j != i) {
+                if (cnt < kNbCap) {
+                    if (kMode == kEmitStaged) s_nb[cnt][t] = j;
+                    if (kMode == kEmitTile) nbr[nbr_index(i, cnt)] = j;
+                }
+                ++cnt;
+            }
+        });
+        const float rho = c.cd * s;
+        rho_out[i] = rho;
+        pr_out[i] = make_float2(pressure_of(c, rho), 1.f / rho);
+        if (kMode != kEmitNone) nbr_count[i] = cnt;
+    }
+    if (kMode == kEmitStaged) {
+        // Copy each warp's recorded rows out in full 128-byte lines.
+        const uint32_t kmax = __reduce_max_sync(0xffffffffu, min(cnt, (uint32_t)kNbCap));
+        uint32_t* tile = nbr + (size_t)blockIdx.x * kNbCap * kNbTile + t;
+        for (uint32_t k = 0; k < kmax; ++k) tile[(size_t)k * kNbTile] = s_nb[k][t];
+    }
+}
+
+template <int kMode, int kBlockSize>
+void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
+    with_reach(c.reach, [&](auto R) {
+        k_density<kMode, kBlockSize, decltype(R)::value><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
+            d.pos, d.cell_start, d.n, c, d.rho, d.pr, d.nbr, d.nbr_count);
+    });
+}
+
+}  // namespace
+
+void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (!d.n) return;
+    const bool big = d.tune.density_block == 256;
+    if (!d.nbr || d.tune.list_mode == SF_LIST_NONE) {
+        big ? density_as<kEmitNone, 256>(d, c, s) : density_as<kEmitNone, 128>(d, c, s);
+    } else if (d.tune.list_mode == SF_LIST_TILE_STAGED) {
+        density_as<kEmitStaged, kNbTile>(d, c, s);
+    } else {
+        big ? density_as<kEmitTile, 256>(d, c, s) : density_as<kEmitTile, 128>(d, c, s);
+    }
+}
+
+}  // namespace sf

@@ -1,0 +1,156 @@
+// sf_device.cuh — device helpers shared by the kernels of the SPH sub-step.
+//
+// The translation units that include this header are compiled with
+// -fmad=false: multiply-adds are fused only where fmaf() is written, so the
+// arithmetic matches the CPU oracle operation for operation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "sf_internal.h"
+
+namespace sf {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// Calls f(std::integral_constant<int, K>) for the context's reach K.
+template <typename F>
+inline void with_reach(int reach, F&& f) {
+    switch (reach) {
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        default: f(std::integral_constant<int, 2>{}); break;
+    }
+}
+
+__device__ __forceinline__ int cell_coord(float x, float bmin, float inv_cell, int n) {
+    const float t = floorf((x - bmin) * inv_cell);
+    return (t >= 0.f) ? ((t < (float)n) ? (int)t : n - 1) : 0;  // NaN -> 0
+}
+
+__device__ __forceinline__ uint32_t cell_key(const SimConst& c, float x, float y, float z) {
+    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
+    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
+    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
+    return ((uint32_t)cz * (uint32_t)c.n[1] + (uint32_t)cy) * (uint32_t)c.n[0] + (uint32_t)cx;
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {  // murmur3 finaliser
+    x ^= x >> 16;
+    x *= 0x85ebca6bu;
+    x ^= x >> 13;
+    x *= 0xc2b2ae35u;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Lower bound, minus the pruning slack, of the axis distance from a point at
+// offset `off` inside its cell (width w) to the cell at offset d.
+__device__ __forceinline__ float face_gap(float off, int d, float w, float margin) {
+    float gap = 0.f;
+    if (d > 0) gap = (float)d * w - off;
+    if (d < 0) gap = off - (float)(d + 1) * w;
+    return fmaxf(gap - margin, 0.f);
+}
+
+// Calls f(j, pos[j]) for the neighbour candidates of a particle at (x, y, z)
+// in the canonical order: dz = -R..R, dy = -R..R, then the contiguous sorted
+// range of the row's cells cx-R..cx+R (R = kReach = cells per kernel radius).
+// Rows and end cells whose nearest face is provably farther than h (by a
+// margin that covers the rounding of cell assignment) are skipped: they hold
+// no neighbour, so skipping them changes no sum and no list.
+template <int kReach, typename F>
+__device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
+                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
+    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
+    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
+    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
+    const float ox = (x - c.bmin[0]) - (float)cx * c.cell_w[0];  // positions inside the cell
+    const float oy = (y - c.bmin[1]) - (float)cy * c.cell_w[1];
+    const float oz = (z - c.bmin[2]) - (float)cz * c.cell_w[2];
+#pragma unroll 1
+    for (int dz = -kReach; dz <= kReach; ++dz) {
+        const int zz = cz + dz;
+        if (zz < 0 || zz >= c.n[2]) continue;
+        const float gz = face_gap(oz, dz, c.cell_w[2], c.prune_margin);
+#pragma unroll 1
+        for (int dy = -kReach; dy <= kReach; ++dy) {
+            const int yy = cy + dy;
+            if (yy < 0 || yy >= c.n[1]) continue;
+            const float gy = face_gap(oy, dy, c.cell_w[1], c.prune_margin);
+            const float g2 = fmaf(gz, gz, gy * gy);
+            if (g2 >= c.prune_h2) continue;
+            int lo = -kReach, hi = kReach;
+            if (kReach > 1) {
+                while (lo < 0) {
+                    const float gx = face_gap(ox, lo, c.cell_w[0], c.prune_margin);
+                    if (fmaf(gx, gx, g2) < c.prune_h2) break;
+                    ++lo;
+                }
+                while (hi > 0) {
+                    const float gx = face_gap(ox, hi, c.cell_w[0], c.prune_margin);
+                    if (fmaf(gx, gx, g2) < c.prune_h2) break;
+                    --hi;
+                }
+            }
+            const int x0 = max(cx + lo, 0), x1 = min(cx + hi, c.n[0] - 1);
+            const uint32_t row = ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
+            const uint32_t b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
+#pragma unroll 1
+            for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+        }
+    }
+}
+
+// Equation of state and the p >= 0 clamp (SPHParameters::bUseAttractivePressure).
+__device__ __forceinline__ float pressure_of(const SimConst& c, float rho) {
+    float p;
+    if (c.eos == SF_EOS_TAIT) {
+        const float x = rho * c.inv_rho0;
+        const float x2 = x * x;
+        const float x4 = x2 * x2;
+        const float x7 = (x4 * x2) * x;
+        p = c.k * (x7 - 1.f);
+    } else {
+        p = c.k * (rho - c.rho0);
+    }
+    if (!c.attractive) p = (p < 0.f) ? 0.f : p;
+    return p;
+}
+
+// Index of particle i's k-th neighbour in the list buffer: tiles of kNbTile
+// particles, k-major inside a tile, so a warp reads one 128-byte line per k.
+__device__ __forceinline__ size_t nbr_index(uint32_t i, uint32_t k) {
+    return ((size_t)(i / kNbTile) * kNbCap + k) * kNbTile + (i % kNbTile);
+}
+
+// Pair terms of particle i with neighbour j (j != i, |xi - xj| < h), in the
+// oracle's operation order.
+struct PairAcc {
+    float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
+};
+
+__device__ __forceinline__ void pair_terms(const SimConst& c, const float4& xi, const float4& vi, float pi,
+                                           const float4& xj, const float2& prj, const float4& vj, PairAcc& a) {
+    const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float r = sqrtf(r2);
+    const float hr = c.h - r;
+    const float w = hr * prj.y;
+    a.avx = fmaf(w, vj.x - vi.x, a.avx);
+    a.avy = fmaf(w, vj.y - vi.y, a.avy);
+    a.avz = fmaf(w, vj.z - vi.z, a.avz);
+    if (r > 0.f) {
+        const float sp = ((pi + prj.x) * w) * (hr / r);
+        a.apx = fmaf(sp, dx, a.apx);
+        a.apy = fmaf(sp, dy, a.apy);
+        a.apz = fmaf(sp, dz, a.apz);
+    }
+}
+
+}  // namespace sf

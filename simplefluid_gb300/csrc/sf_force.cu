@@ -1,0 +1,115 @@
+// sf_force.cu — force + integration pass of the SPH sub-step (sm_103a).
+//
+// One thread per cell-sorted particle.  Pressure (spiky gradient, symmetrised
+// (p_i + p_j) / (2 rho_j) weight), viscosity (Laplacian) and gravity from the
+// neighbour list of the density pass — or from a rescan of the candidate cells
+// where the list overflowed or no list was recorded — then, in the stepping
+// variant, symplectic Euler, the box clamp with restitution and the next
+// step's cell key and arrival slot (the counting sort's histogram).
+// kPrefetch neighbours are gathered before their terms are added, so the
+// dependent index -> data loads overlap; the terms are still added in list
+// order, which keeps the sum bit-identical.
+#include "sf_device.cuh"
+
+namespace sf {
+namespace {
+
+template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kReach>
+__global__ void __launch_bounds__(kBlockSize)
+    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
+            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+            uint32_t n, SimConst c, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+            uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out) {
+    const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = pos[i];
+    const float4 vi = vel[i];
+    const float2 pri = pr[i];
+    PairAcc a;
+    const uint32_t cnt = kUseList ? nbr_count[i] : 0xffffffffu;
+    if (cnt <= (uint32_t)kNbCap) {
+        uint32_t k = 0;
+        for (; k + kPrefetch <= cnt; k += kPrefetch) {
+            uint32_t j[kPrefetch];
+            float4 xj[kPrefetch], vj[kPrefetch];
+            float2 pj[kPrefetch];
+#pragma unroll
+            for (int u = 0; u < kPrefetch; ++u) j[u] = __ldg(nbr + nbr_index(i, k + u));
+#pragma unroll
+            for (int u = 0; u < kPrefetch; ++u) {
+                xj[u] = ldg4(pos + j[u]);
+                vj[u] = ldg4(vel + j[u]);
+                pj[u] = __ldg(pr + j[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kPrefetch; ++u) pair_terms(c, xi, vi, pri.x, xj[u], pj[u], vj[u], a);
+        }
+        for (; k < cnt; ++k) {
+            const uint32_t j = __ldg(nbr + nbr_index(i, k));
+            pair_terms(c, xi, vi, pri.x, ldg4(pos + j), __ldg(pr + j), ldg4(vel + j), a);
+        }
+    } else {
+        for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+            if (j == i) return;
+            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+            if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)
+                pair_terms(c, xi, vi, pri.x, xj, __ldg(pr + j), ldg4(vel + j), a);
+        });
+    }
+    const float ax = fmaf(fmaf(c.cp, a.apx, c.cv * a.avx), pri.y, c.g[0]);
+    const float ay = fmaf(fmaf(c.cp, a.apy, c.cv * a.avy), pri.y, c.g[1]);
+    const float az = fmaf(fmaf(c.cp, a.apz, c.cv * a.avz), pri.y, c.g[2]);
+    if (!kIntegrate) {
+        acc_out[i] = make_float4(ax, ay, az, 0.f);
+        return;
+    }
+    float v[3] = {fmaf(c.dt, ax, vi.x), fmaf(c.dt, ay, vi.y), fmaf(c.dt, az, vi.z)};
+    float x[3] = {fmaf(c.dt, v[0], xi.x), fmaf(c.dt, v[1], xi.y), fmaf(c.dt, v[2], xi.z)};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        if (x[q] < c.lo[q]) {
+            x[q] = c.lo[q];
+            if (v[q] < 0.f) v[q] = -c.e * v[q];
+        }
+        if (x[q] > c.hi[q]) {
+            x[q] = c.hi[q];
+            if (v[q] > 0.f) v[q] = -c.e * v[q];
+        }
+    }
+    pos_out[i] = make_float4(x[0], x[1], x[2], xi.w);
+    vel_out[i] = make_float4(v[0], v[1], v[2], 0.f);
+    const uint32_t key = cell_key(c, x[0], x[1], x[2]);
+    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+}
+
+template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate>
+void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    with_reach(c.reach, [&](auto R) {
+        k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, decltype(R)::value>
+            <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
+                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, kIntegrate ? d.pos2 : nullptr,
+                kIntegrate ? d.vel2 : nullptr, kIntegrate ? d.counts : nullptr, kIntegrate ? d.key_slot : nullptr,
+                kIntegrate ? nullptr : d.accel);
+    });
+}
+
+template <bool kIntegrate>
+void launch_force(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (!d.n) return;
+    const bool big = d.tune.force_block == 256;
+    if (!d.nbr || d.tune.list_mode == SF_LIST_NONE) {
+        big ? force_as<false, 2, 256, kIntegrate>(d, c, s) : force_as<false, 2, 128, kIntegrate>(d, c, s);
+    } else if (d.tune.prefetch == 2) {
+        big ? force_as<true, 2, 256, kIntegrate>(d, c, s) : force_as<true, 2, 128, kIntegrate>(d, c, s);
+    } else {
+        big ? force_as<true, 4, 256, kIntegrate>(d, c, s) : force_as<true, 4, 128, kIntegrate>(d, c, s);
+    }
+}
+
+}  // namespace
+
+void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s) { launch_force<true>(d, c, s); }
+
+void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s) { launch_force<false>(d, c, s); }
+
+}  // namespace sf

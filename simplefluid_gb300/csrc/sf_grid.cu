@@ -1,78 +1,17 @@
-// sf_kernels.cu — sm_103a kernels of the SPH sub-step.
+// sf_grid.cu — uniform-grid neighbour search of the SPH sub-step (sm_103a):
+// cell hashing, the counting sort with its cell table, particle reorder, state
+// upload/download, and the stage list of one sub-step.
 //
-// One sub-step (the body of SPHSolver<float>::advanceFrame, called at
-// Source/Simulator.cpp:49 of the reference) on particles kept in cell-sorted
-// order:
-//   k_density          poly6 density + equation of state        (1 thread / particle)
-//   k_force<true>      spiky pressure + viscosity + gravity, symplectic Euler,
-//                      box clamp with restitution, next cell key + arrival slot
-//   k_scan_*           counts -> cell_start (exclusive scan), counts := 0
-//   k_scatter          bucket unsorted indices by cell
-//   k_rank_gather      stable rank inside each cell, gather pos/vel to sorted slots
-// The sort is a one-pass counting (radix-`ncells`) sort: its histogram is the
-// cell table, so cell start/end come out of the same scan.  Stability (equal
-// keys keep their previous order) is restored by ranking each particle among
-// its cell's members, which makes the order deterministic and identical to a
-// stable sort.
-//
-// This translation unit is compiled with -fmad=false: multiply-adds are fused
-// only where fmaf() is written, so the arithmetic matches the CPU oracle
-// operation for operation.
-#include <cuda_runtime.h>
-
-#include "sf_internal.h"
+// The sort is a one-pass counting (radix-`ncells`) sort: the histogram of cell
+// keys, taken by the force pass's atomics (k_hash_count for an uploaded
+// state), is exclusive-scanned into the cell table, so cell start/end come out
+// of the same scan that places the particles.  Stability (equal keys keep their
+// previous order) is restored by ranking each particle among its cell's
+// members, which makes the order deterministic and identical to a stable sort.
+#include "sf_device.cuh"
 
 namespace sf {
 namespace {
-
-constexpr int kBlock = 256;
-
-__device__ __forceinline__ int cell_coord(float x, float bmin, float inv_cell, int n) {
-    const float t = floorf((x - bmin) * inv_cell);
-    return (t >= 0.f) ? ((t < (float)n) ? (int)t : n - 1) : 0;  // NaN -> 0
-}
-
-__device__ __forceinline__ uint32_t cell_key(const SimConst& c, float x, float y, float z) {
-    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
-    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
-    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
-    return ((uint32_t)cz * (uint32_t)c.n[1] + (uint32_t)cy) * (uint32_t)c.n[0] + (uint32_t)cx;
-}
-
-__device__ __forceinline__ uint32_t mix32(uint32_t x) {
-    x ^= x >> 16;
-    x *= 0x85ebca6bu;
-    x ^= x >> 13;
-    x *= 0xc2b2ae35u;
-    x ^= x >> 16;
-    return x;
-}
-
-__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
-
-// Calls f(j) for the neighbour candidates of a particle at (x, y, z) in the
-// canonical order: dz = -1..1, dy = -1..1, then the contiguous sorted range of
-// the row's cells cx-1..cx+1.
-template <typename F>
-__device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs, float x, float y,
-                                               float z, F&& f) {
-    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
-    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
-    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
-    const int x0 = max(cx - 1, 0), x1 = min(cx + 1, c.n[0] - 1);
-#pragma unroll 1
-    for (int zz = cz - 1; zz <= cz + 1; ++zz) {
-        if (zz < 0 || zz >= c.n[2]) continue;
-#pragma unroll 1
-        for (int yy = cy - 1; yy <= cy + 1; ++yy) {
-            if (yy < 0 || yy >= c.n[1]) continue;
-            const uint32_t row = ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
-            const uint32_t b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
-#pragma unroll 2
-            for (uint32_t j = b; j < e; ++j) f(j);
-        }
-    }
-}
 
 // ---------------------------------------------------------------- state IO
 __global__ void k_load_aos(const float* __restrict__ pos3, const float* __restrict__ vel3, uint32_t n,
@@ -174,7 +113,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(uint32_t* __restric
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint4* __restrict__ counts,
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint4* __restrict__ counts,
                                                              const uint32_t* __restrict__ tile_sums,
                                                              uint4* __restrict__ cell_start) {
     __shared__ uint32_t total;
@@ -182,16 +121,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint4* __restrict__
     const uint4 q = counts[t];
     const uint32_t ex = block_exclusive(q.x + q.y + q.z + q.w, &total) + tile_sums[blockIdx.x];
     cell_start[t] = make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
-    counts[t] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // ---------------------------------------------------------------- reorder
+// Buckets indices by cell and clears the occupied cells' counters for the next
+// step (only occupied cells were counted, so this leaves all counters zero).
 __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start, uint32_t n,
-                          uint32_t* __restrict__ tmp) {
+                          uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 ks = key_slot[i];
     tmp[cell_start[ks.x] + ks.y] = i;
+    counts[ks.x] = 0u;
 }
 
 __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start,
@@ -209,110 +150,16 @@ __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t
     vel_out[dst] = vel_in[i];
 }
 
-// ---------------------------------------------------------------- density
-__global__ void __launch_bounds__(kBlock) k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs,
-                                                    uint32_t n, SimConst c, float* __restrict__ rho_out,
-                                                    float2* __restrict__ pr_out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 xi = pos[i];
-    float s = 0.f;
-    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
-        const float4 xj = ldg4(pos + j);
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        if (r2 < c.h2) {
-            const float q = c.h2 - r2;
-            s = fmaf(q * q, q, s);
-        }
-    });
-    const float rho = c.cd * s;
-    float p;
-    if (c.eos == SF_EOS_TAIT) {
-        const float x = rho * c.inv_rho0;
-        const float x2 = x * x;
-        const float x4 = x2 * x2;
-        const float x7 = (x4 * x2) * x;
-        p = c.k * (x7 - 1.f);
-    } else {
-        p = c.k * (rho - c.rho0);
-    }
-    if (!c.attractive) p = (p < 0.f) ? 0.f : p;
-    rho_out[i] = rho;
-    pr_out[i] = make_float2(p, 1.f / rho);
-}
-
-// ---------------------------------------------------------------- forces
-template <bool kIntegrate>
-__global__ void __launch_bounds__(kBlock)
-    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
-            const uint32_t* __restrict__ cs, uint32_t n, SimConst c, float4* __restrict__ pos_out,
-            float4* __restrict__ vel_out, uint32_t* __restrict__ counts, uint2* __restrict__ key_slot,
-            float4* __restrict__ acc_out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 xi = pos[i];
-    const float4 vi = vel[i];
-    const float2 pri = pr[i];
-    float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
-    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
-        if (j == i) return;
-        const float4 xj = ldg4(pos + j);
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        if (r2 < c.h2) {
-            const float r = sqrtf(r2);
-            const float hr = c.h - r;
-            const float2 prj = __ldg(pr + j);
-            const float4 vj = ldg4(vel + j);
-            const float w = hr * prj.y;
-            avx = fmaf(w, vj.x - vi.x, avx);
-            avy = fmaf(w, vj.y - vi.y, avy);
-            avz = fmaf(w, vj.z - vi.z, avz);
-            if (r > 0.f) {
-                const float sp = ((pri.x + prj.x) * w) * (hr / r);
-                apx = fmaf(sp, dx, apx);
-                apy = fmaf(sp, dy, apy);
-                apz = fmaf(sp, dz, apz);
-            }
-        }
-    });
-    const float ax = fmaf(fmaf(c.cp, apx, c.cv * avx), pri.y, c.g[0]);
-    const float ay = fmaf(fmaf(c.cp, apy, c.cv * avy), pri.y, c.g[1]);
-    const float az = fmaf(fmaf(c.cp, apz, c.cv * avz), pri.y, c.g[2]);
-    if (!kIntegrate) {
-        acc_out[i] = make_float4(ax, ay, az, 0.f);
-        return;
-    }
-    float v[3] = {fmaf(c.dt, ax, vi.x), fmaf(c.dt, ay, vi.y), fmaf(c.dt, az, vi.z)};
-    float x[3] = {fmaf(c.dt, v[0], xi.x), fmaf(c.dt, v[1], xi.y), fmaf(c.dt, v[2], xi.z)};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (x[a] < c.lo[a]) {
-            x[a] = c.lo[a];
-            if (v[a] < 0.f) v[a] = -c.e * v[a];
-        }
-        if (x[a] > c.hi[a]) {
-            x[a] = c.hi[a];
-            if (v[a] > 0.f) v[a] = -c.e * v[a];
-        }
-    }
-    pos_out[i] = make_float4(x[0], x[1], x[2], xi.w);
-    vel_out[i] = make_float4(v[0], v[1], v[2], 0.f);
-    const uint32_t key = cell_key(c, x[0], x[1], x[2]);
-    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
-}
-
 // ---------------------------------------------------------------- inspection
+template <int kReach>
 __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n,
                                   SimConst c, uint32_t* __restrict__ count, uint32_t* __restrict__ hash) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 xi = pos[i];
     uint32_t cnt = 0, h = 0;
-    for_candidates(c, cs, xi.x, xi.y, xi.z, [&](uint32_t j) {
+    for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
         if (j == i) return;
-        const float4 xj = ldg4(pos + j);
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2) {
             ++cnt;
@@ -322,8 +169,6 @@ __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t
     count[i] = cnt;
     hash[i] = h;
 }
-
-inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
 
@@ -352,7 +197,7 @@ static void launch_scan_tiles(DeviceState& d, cudaStream_t s) {
     k_scan_tiles<<<1, kScanThreads, 0, s>>>(d.tile_sums, d.ntiles);
 }
 static void launch_scan_apply(DeviceState& d, cudaStream_t s) {
-    k_scan_apply<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<uint4*>(d.counts), d.tile_sums,
+    k_scan_apply<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
                                                    reinterpret_cast<uint4*>(d.cell_start));
 }
 
@@ -362,8 +207,9 @@ void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
     launch_scan_apply(d, s);
 }
 
-void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, cudaStream_t s) {
-    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp);
+void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
+                    cudaStream_t s) {
+    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts);
 }
 
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
@@ -373,30 +219,18 @@ void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const
                                                              vel_out);
 }
 
-void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s) {
-    if (d.n) k_density<<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, d.rho, d.pr);
-}
-
-void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s) {
-    if (d.n)
-        k_force<true><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.n, c, d.pos2,
-                                                               d.vel2, d.counts, d.key_slot, nullptr);
-}
-
-void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s) {
-    if (d.n)
-        k_force<false><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.n, c, nullptr,
-                                                                nullptr, nullptr, nullptr, d.accel);
-}
-
 void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
                             cudaStream_t s) {
-    if (d.n) k_neighbour_stats<<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, count, hash);
+    if (!d.n) return;
+    with_reach(c.reach, [&](auto R) {
+        k_neighbour_stats<decltype(R)::value>
+            <<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, count, hash);
+    });
 }
 
 void enqueue_sort_tail(DeviceState& d, cudaStream_t s) {
     launch_scan_cells(d, d.n, s);
-    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, s);
+    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s);
     launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
 }
 
@@ -410,7 +244,7 @@ void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream
         case 2: launch_scan_reduce(d, s); break;
         case 3: launch_scan_tiles(d, s); break;
         case 4: launch_scan_apply(d, s); break;
-        case 5: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, s); break;
+        case 5: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s); break;
         case 6: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
         default: break;
     }

@@ -23,8 +23,15 @@ struct SimConst {
     float inv_cell[3];    // cells per unit length, per axis
     int n[3];             // cells per axis
     int eos, attractive;
+    int reach;            // cells searched on each side: K = cells per kernel radius
     uint32_t ncells;
     float mass;
+    // Conservative pruning of the candidate walk (skips only cells that hold
+    // no particle within h): cell widths, a slack covering the rounding of
+    // cell assignment, and the squared-distance threshold h^2 (1 + 1e-4).
+    float cell_w[3];
+    float prune_margin;
+    float prune_h2;
 };
 
 // Fill `c` from `p`; returns SF_OK or an error code (with message in `why`).
@@ -33,8 +40,17 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why);
 // Scene generator (sf_scenes.cpp): AoS float3 positions of `scene`.
 int scene_points(const sf_params& p, int scene, uint64_t seed, std::vector<float>& out, const char** why);
 
+// Kernel choices of a context (all give bit-identical results).
+struct Tuning {
+    int list_mode = SF_LIST_TILE;  // SF_LIST_*: how the density pass records neighbours
+    int density_block = 256;       // 128 or 256 threads
+    int force_block = 256;         // 128 or 256 threads
+    int prefetch = 2;              // neighbours gathered per batch in the force pass: 2 or 4
+};
+
 // Device buffers of one solver context (all owned by the context).
 struct DeviceState {
+    Tuning tune;
     uint32_t n = 0, cap = 0;
     float4* pos = nullptr;   // sorted positions, w = original index (bit pattern)
     float4* vel = nullptr;   // sorted velocities, w = 0
@@ -46,6 +62,8 @@ struct DeviceState {
     uint32_t* tmp = nullptr;    // cell-bucketed unsorted indices
     float* io = nullptr;        // AoS staging, 6 floats per particle
     float4* accel = nullptr;    // optional acceleration output (inspection)
+    uint32_t* nbr = nullptr;       // neighbour lists, tile-major (kNbCap * kNbTile per tile)
+    uint32_t* nbr_count = nullptr; // neighbours of each particle (may exceed kNbCap)
     // grid
     uint32_t ncells = 0, ncells_pad = 0;
     uint32_t* counts = nullptr;      // ncells_pad, zero between steps
@@ -53,6 +71,13 @@ struct DeviceState {
     uint32_t* tile_sums = nullptr;   // one per scan tile
     uint32_t ntiles = 0;
 };
+
+// Neighbour lists: up to kNbCap neighbours per particle, in tiles of kNbTile
+// particles (see nbr_index in sf_device.cuh).
+constexpr int kNbTile = 128;
+constexpr int kNbCap = 64;
+// list emission modes of the density pass
+constexpr int kEmitNone = 0, kEmitStaged = 1, kEmitTile = 2;
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
@@ -64,7 +89,8 @@ void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* p
 void launch_hash_count(const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts, uint2* key_slot,
                        cudaStream_t s);
 void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
-void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, cudaStream_t s);
+void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
+                    cudaStream_t s);
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
                         const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s);
 void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
@@ -77,7 +103,7 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
                             cudaStream_t s);
 
 // The sort tail shared by makeReady and every step: counts -> cell_start,
-// bucket, stable rank, gather pos2/vel2 -> pos/vel.
+// bucket (clearing the counters), stable rank, gather pos2/vel2 -> pos/vel.
 void enqueue_sort_tail(DeviceState& d, cudaStream_t s);
 // One full sub-step on the sorted state.
 void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);

@@ -50,6 +50,7 @@ class SPHParameters:
     boxMin: tuple = (0.0, 0.0, 0.0)
     boxMax: tuple = (1.0, 1.0, 1.0)
     eos: int = C.SF_EOS_LINEAR
+    cellsPerH: int = 2
 
     def to_c(self) -> C.sf_params:
         p = C.sf_params()
@@ -69,6 +70,7 @@ class SPHParameters:
             p.box_max[a] = self.boxMax[a]
         p.time_step = self.timeStep
         p.eos = int(self.eos)
+        p.cells_per_h = int(self.cellsPerH)
         return p
 
     @classmethod
@@ -77,7 +79,7 @@ class SPHParameters:
                    pressureStiffness=p.pressure_stiffness, boundaryRestitution=p.boundary_restitution,
                    viscosity=p.viscosity, stopTime=p.stop_time, bUseAttractivePressure=bool(p.use_attractive_pressure),
                    scene=p.scene, restDensity=p.rest_density, gravity=tuple(p.gravity), timeStep=p.time_step,
-                   boxMin=tuple(p.box_min), boxMax=tuple(p.box_max), eos=p.eos)
+                   boxMin=tuple(p.box_min), boxMax=tuple(p.box_max), eos=p.eos, cellsPerH=p.cells_per_h)
 
     def updateParams(self) -> None:
         """SPHParameters::updateParams() (Source/Controller.cpp:63): validate."""

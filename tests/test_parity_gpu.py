@@ -287,7 +287,7 @@ def test_set_params_regrids(oracle):
         prm2 = params_16k(kernelRadius=0.05)
         s.setParams(prm2)
         d = oracle.derive(prm2.to_c())
-        assert s.gridDims() == (int(d["nx"]), int(d["ny"]), int(d["nz"])) == (19, 19, 19)
+        assert s.gridDims() == (int(d["nx"]), int(d["ny"]), int(d["nz"])) == (39, 39, 39)
         gcnt, ghash = s.neighbourStats()
         _, _, gids, _ = s.sortedState()
     # the solver re-sorts its current (old-grid) order stably on the new grid
@@ -327,3 +327,44 @@ def test_full_size_1m_double_dambreak(oracle):
     assert cs[0] == 0 and cs[-1] == n and np.array_equal(np.diff(cs.astype(np.int64)), counts)
     assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
     assert np.all(gpos >= np.float32(0.0025)) and np.all(gpos <= np.float32(0.9975))
+
+
+def _tuned_run(prm, pos, tune, steps):
+    import ctypes
+    lib = C.load()
+    with solver_with(prm, pos) as s:
+        C.check(lib.sf_set_tuning(s.handle, ctypes.byref(tune)))
+        got = C.sf_tuning()
+        C.check(lib.sf_get_tuning(s.handle, ctypes.byref(got)))
+        assert bytes(got) == bytes(tune)
+        s.step(steps)
+        return s.getState()
+
+
+def test_tuning_variants_are_bit_identical(oracle):
+    """Every kernel choice (neighbour-list layout, block sizes, gather batch)
+    computes the same bits; a dense cluster forces the list-overflow path."""
+    prm = params_16k()
+    pos = jittered_block(n_side=(16, 20, 16), seed=12)
+    rng = np.random.default_rng(12)
+    cluster = (0.7 + rng.uniform(0, 0.03, size=(200, 3))).astype(np.float32)
+    pos = np.concatenate([pos, cluster])
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 8)
+    st.sort(prm.to_c())
+    ref_pos, ref_vel = st.original_order()
+    combos = [(m, db, fb, pf) for m in (0, 1, 2) for db in (128, 256) for fb in (128, 256) for pf in (2, 4)
+              if not (m == 0 and pf != 2) and not (m == 1 and db != 128)]
+    for m, db, fb, pf in combos:
+        t = C.sf_tuning(m, db, fb, pf)
+        gpos, gvel = _tuned_run(prm, pos, t, 8)
+        assert np.array_equal(gpos.view(np.uint32), ref_pos.view(np.uint32)), (m, db, fb, pf)
+        assert np.array_equal(gvel.view(np.uint32), ref_vel.view(np.uint32)), (m, db, fb, pf)
+
+
+def test_tuning_rejects_bad_values(lib):
+    import ctypes
+    s = SPHSolver(params_16k())
+    for bad in (C.sf_tuning(7, 128, 128, 2), C.sf_tuning(1, 64, 128, 2), C.sf_tuning(1, 128, 128, 3)):
+        assert lib.sf_set_tuning(s.handle, ctypes.byref(bad)) == C.SF_ERR_INVALID_ARGUMENT
+    s.close()
