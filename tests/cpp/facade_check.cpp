@@ -1,0 +1,56 @@
+// Drives the C++ façade the way the reference's Simulator does
+// (Source/Simulator.cpp:33-63, 85-103): setupScene -> makeReady ->
+// advanceFrame until the frame's 1/30 s accumulates, for `frames` frames.
+// Writes the final positions and velocities (caller order, float32) to the
+// output file.  Used by tests/test_facade.py.
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+
+#include "simplefluid/SPHSolver.hpp"
+
+int main(int argc, char** argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: %s <scene> <frames> <out.bin>\n", argv[0]);
+        return 2;
+    }
+    try {
+        simplefluid::Simulator sim;
+        auto params = sim.getSimParams();
+        params->scene = std::atoi(argv[1]);
+        const int frames = std::atoi(argv[2]);
+        params->stopTime = 0.0333333333f * (float)frames - 1e-6f;
+        int substeps = 0, nframes = 0;
+        unsigned int nparticles = 0;
+        sim.particleChanged = [&] { ++substeps; };
+        sim.frameFinished = [&] { ++nframes; };
+        sim.numParticleChanged = [&](unsigned int n) { nparticles = n; };
+        sim.setupScene();
+        substeps = 0;
+        sim.startSimulation();
+        sim.wait();
+        const auto& pos = sim.solver().particles();
+        const auto& vel = sim.solver().velocity();
+        std::ofstream out(argv[3], std::ios::binary);
+        const uint32_t n = (uint32_t)pos.size();
+        out.write(reinterpret_cast<const char*>(&n), sizeof(n));
+        out.write(reinterpret_cast<const char*>(&substeps), sizeof(substeps));
+        out.write(reinterpret_cast<const char*>(&nframes), sizeof(nframes));
+        out.write(reinterpret_cast<const char*>(pos.data()), n * sizeof(simplefluid::Vec3f));
+        out.write(reinterpret_cast<const char*>(vel.data()), n * sizeof(simplefluid::Vec3f));
+        std::printf("particles=%u substeps=%d frames=%d simtime=%.6f\n", nparticles, substeps, nframes, sim.simTime());
+        // the error path: an invalid parameter throws simplefluid::Error
+        try {
+            params->kernelRadius = -1.f;
+            params->updateParams();
+            std::fprintf(stderr, "expected an error\n");
+            return 1;
+        } catch (const simplefluid::Error& e) {
+            if (e.status != SF_ERR_INVALID_ARGUMENT) return 1;
+        }
+    } catch (const simplefluid::Error& e) {
+        std::fprintf(stderr, "error %d: %s\n", e.status, e.what());
+        return 1;
+    }
+    return 0;
+}
