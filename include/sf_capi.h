@@ -208,6 +208,40 @@ SF_API const char* sf_stage_name(uint32_t stage);
 SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
                                   uint32_t nstages);
 
+/* ---- batches of independent scenes -------------------------------------
+ * Not in the reference (which runs one scene): many independent scenes of
+ * uneven size, each with its own parameters and box, advanced together — one
+ * CUDA-graph launch per step covers every scene.  Scenes must share
+ * cells_per_h (1 or 2).  Particle arrays are the scenes' particles
+ * concatenated in scene order, host AoS float3. */
+typedef struct sf_batch sf_batch;
+/* The batched-cube workload: nscenes scenes drawn from `seed` (counts
+ * log-uniform in [2000, 65536], viscosity U[0.005, 0.05], stiffness
+ * U[20, 100]); a falling lattice block centred in a box of twice its size.
+ * Call with pos_xyz = NULL to learn *total_out first. */
+SF_API sf_status sf_batch_cubes(uint64_t seed, uint32_t nscenes, const sf_params* base, sf_params* params_out,
+                                uint32_t* counts_out, float* pos_xyz, uint64_t capacity, uint64_t* total_out);
+SF_API sf_status sf_batch_create(const sf_params* per_scene, uint32_t nscenes, sf_batch** out);
+SF_API sf_status sf_batch_destroy(sf_batch* b);
+SF_API sf_status sf_batch_num_scenes(const sf_batch* b, uint32_t* n_out);
+SF_API sf_status sf_batch_get_params(const sf_batch* b, uint32_t scene, sf_params* p);
+SF_API sf_status sf_batch_set_state(sf_batch* b, const uint32_t* counts, const float* pos_xyz, const float* vel_xyz);
+SF_API sf_status sf_batch_get_state(sf_batch* b, float* pos_xyz, float* vel_xyz, uint32_t n);
+SF_API sf_status sf_batch_num_particles(const sf_batch* b, uint32_t* n_out);
+/* `nsteps` sub-steps of every scene: one graph launch per step. */
+SF_API sf_status sf_batch_step(sf_batch* b, uint32_t nsteps);
+SF_API sf_status sf_batch_synchronize(sf_batch* b);
+SF_API sf_status sf_batch_step_timed(sf_batch* b, uint32_t nsteps, uint64_t flush_bytes, float* total_ms,
+                                     float* step_ms);
+SF_API sf_status sf_batch_get_tuning(const sf_batch* b, sf_tuning* t);
+SF_API sf_status sf_batch_set_tuning(sf_batch* b, const sf_tuning* t);
+/* Re-grid every scene with K cells per kernel radius (1 or 2). */
+SF_API sf_status sf_batch_set_cells_per_h(sf_batch* b, int32_t cells_per_h);
+/* Autotuner: try every grid granularity and kernel variant for `trial_steps`
+ * steps from the current state, keep the fastest, restore the state. */
+SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning* chosen, int32_t* chosen_cells_per_h,
+                                   float* chosen_ms_per_step);
+
 /* ---- allocation-free density ----------------------------------------------
  * No counterpart in the reference: an addition of this library for callers
  * that cannot allocate device memory (an application or plugin that owns a

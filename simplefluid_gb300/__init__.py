@@ -7,6 +7,8 @@ reference's ``SPHParameters`` / ``SPHSolver`` / ``SceneManager`` / ``Simulator``
 from ._capi import SFError, load  # noqa: F401
 from .solver import (  # noqa: F401
     FRAME_TIME,
+    SPHBatch,
+    batch_cubes,
     SceneManager,
     Simulator,
     SPHParameters,
@@ -15,5 +17,5 @@ from .solver import (  # noqa: F401
     substeps_per_frame,
 )
 
-__all__ = ["SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
+__all__ = ["SPHBatch", "batch_cubes", "SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
            "substeps_per_frame", "FRAME_TIME", "load"]

@@ -115,6 +115,22 @@ PROTOTYPES = {
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
     "sf_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_batch_cubes": (c_int32, [c_uint64, c_uint32, _P(sf_params), c_void_p, c_void_p, c_void_p, c_uint64,
+                                 _P(c_uint64)]),
+    "sf_batch_create": (c_int32, [c_void_p, c_uint32, _P(c_void_p)]),
+    "sf_batch_destroy": (c_int32, [c_void_p]),
+    "sf_batch_num_scenes": (c_int32, [c_void_p, _P(c_uint32)]),
+    "sf_batch_get_params": (c_int32, [c_void_p, c_uint32, _P(sf_params)]),
+    "sf_batch_set_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sf_batch_get_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_batch_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
+    "sf_batch_step": (c_int32, [c_void_p, c_uint32]),
+    "sf_batch_synchronize": (c_int32, [c_void_p]),
+    "sf_batch_step_timed": (c_int32, [c_void_p, c_uint32, c_uint64, _P(c_float), c_void_p]),
+    "sf_batch_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_batch_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_batch_set_cells_per_h": (c_int32, [c_void_p, c_int32]),
+    "sf_batch_autotune": (c_int32, [c_void_p, c_uint32, _P(sf_tuning), _P(c_int32), _P(c_float)]),
     "sf_density_noalloc": (c_int32, [_P(sf_params), c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
 }
 

@@ -16,9 +16,10 @@
 namespace sf {
 namespace {
 
-template <int kMode, int kBlockSize, int kReach>
+template <int kMode, int kBlockSize, int kReach, bool kBatched>
 __global__ void __launch_bounds__(kBlockSize)
-    k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n, SimConst c,
+    k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n, SimConst c0,
+              const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
               float* __restrict__ rho_out, float2* __restrict__ pr_out, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count) {
     __shared__ uint32_t s_nb[kMode == kEmitStaged ? kNbCap : 1][kMode == kEmitStaged ? kBlockSize : 1];
@@ -26,6 +27,7 @@ __global__ void __launch_bounds__(kBlockSize)
     const uint32_t i = blockIdx.x * kBlockSize + t;
     uint32_t cnt = 0;
     if (i < n) {
+        const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
         const float4 xi = pos[i];
         float s = 0.f;
         for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
@@ -58,8 +60,15 @@ __global__ void __launch_bounds__(kBlockSize)
 template <int kMode, int kBlockSize>
 void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
     with_reach(c.reach, [&](auto R) {
-        k_density<kMode, kBlockSize, decltype(R)::value><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-            d.pos, d.cell_start, d.n, c, d.rho, d.pr, d.nbr, d.nbr_count);
+        constexpr int K = decltype(R)::value;
+        if (d.table) {
+            if constexpr (K <= 2)
+                k_density<kMode, kBlockSize, K, true><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
+                    d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, d.rho, d.pr, d.nbr, d.nbr_count);
+        } else {
+            k_density<kMode, kBlockSize, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
+                d.pos, d.cell_start, d.n, c, nullptr, nullptr, 0, d.rho, d.pr, d.nbr, d.nbr_count);
+        }
     });
 }
 

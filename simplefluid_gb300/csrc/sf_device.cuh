@@ -35,7 +35,28 @@ __device__ __forceinline__ uint32_t cell_key(const SimConst& c, float x, float y
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
     const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
     const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
-    return ((uint32_t)cz * (uint32_t)c.n[1] + (uint32_t)cy) * (uint32_t)c.n[0] + (uint32_t)cx;
+    return c.cell_base + ((uint32_t)cz * (uint32_t)c.n[1] + (uint32_t)cy) * (uint32_t)c.n[0] + (uint32_t)cx;
+}
+
+// Scene of particle i in a batch: the last s with scene_off[s] <= i.
+__device__ __forceinline__ uint32_t scene_of(const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t i) {
+    uint32_t lo = 0, hi = nscenes;  // invariant: scene_off[lo] <= i < scene_off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(scene_off + mid) <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Constants of particle i: the launch's own, or its scene's in a batch.
+template <bool kBatched>
+__device__ __forceinline__ SimConst const_of(const SimConst& c0, const SimConst* __restrict__ table,
+                                             const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t i) {
+    if (!kBatched) return c0;
+    return table[scene_of(scene_off, nscenes, i)];
 }
 
 __device__ __forceinline__ uint32_t mix32(uint32_t x) {  // murmur3 finaliser
@@ -99,7 +120,7 @@ __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t
                 }
             }
             const int x0 = max(cx + lo, 0), x1 = min(cx + hi, c.n[0] - 1);
-            const uint32_t row = ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
+            const uint32_t row = c.cell_base + ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
             const uint32_t b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
 #pragma unroll 1
             for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));

@@ -14,14 +14,16 @@
 namespace sf {
 namespace {
 
-template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kReach>
+template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kReach, bool kBatched>
 __global__ void __launch_bounds__(kBlockSize)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-            uint32_t n, SimConst c, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+            uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
+            uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out) {
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     if (i >= n) return;
+    const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 xi = pos[i];
     const float4 vi = vel[i];
     const float2 pri = pr[i];
@@ -85,11 +87,23 @@ __global__ void __launch_bounds__(kBlockSize)
 template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate>
 void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
     with_reach(c.reach, [&](auto R) {
-        k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, decltype(R)::value>
-            <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, kIntegrate ? d.pos2 : nullptr,
-                kIntegrate ? d.vel2 : nullptr, kIntegrate ? d.counts : nullptr, kIntegrate ? d.key_slot : nullptr,
-                kIntegrate ? nullptr : d.accel);
+        constexpr int K = decltype(R)::value;
+        float4* po = kIntegrate ? d.pos2 : nullptr;
+        float4* vo = kIntegrate ? d.vel2 : nullptr;
+        uint32_t* co = kIntegrate ? d.counts : nullptr;
+        uint2* ks = kIntegrate ? d.key_slot : nullptr;
+        float4* ac = kIntegrate ? nullptr : d.accel;
+        if (d.table) {
+            if constexpr (K <= 2 && kPrefetch == 2)
+                k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>
+                    <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.nbr,
+                                                                     d.nbr_count, d.n, c, d.table, d.scene_off,
+                                                                     d.nscenes, po, vo, co, ks, ac);
+        } else {
+            k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
+                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ks,
+                ac);
+        }
     });
 }
 

@@ -46,18 +46,24 @@ __global__ void k_store_aos(const float4* __restrict__ pos, const float4* __rest
 }
 
 // ---------------------------------------------------------------- hashing
-__global__ void k_hash_count(const float4* __restrict__ pos, uint32_t n, SimConst c, uint32_t* __restrict__ counts,
+template <bool kBatched>
+__global__ void k_hash_count(const float4* __restrict__ pos, uint32_t n, SimConst c0, const SimConst* __restrict__ table,
+                             const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t* __restrict__ counts,
                              uint2* __restrict__ key_slot) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 p = pos[i];
     const uint32_t key = cell_key(c, p.x, p.y, p.z);
     key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
 }
 
-__global__ void k_keys(const float4* __restrict__ pos, uint32_t n, SimConst c, uint32_t* __restrict__ keys) {
+template <bool kBatched>
+__global__ void k_keys(const float4* __restrict__ pos, uint32_t n, SimConst c0, const SimConst* __restrict__ table,
+                       const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t* __restrict__ keys) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 p = pos[i];
     keys[i] = cell_key(c, p.x, p.y, p.z);
 }
@@ -151,11 +157,13 @@ __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t
 }
 
 // ---------------------------------------------------------------- inspection
-template <int kReach>
+template <int kReach, bool kBatched>
 __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n,
-                                  SimConst c, uint32_t* __restrict__ count, uint32_t* __restrict__ hash) {
+                                  SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
+                                  uint32_t nscenes, uint32_t* __restrict__ count, uint32_t* __restrict__ hash) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 xi = pos[i];
     uint32_t cnt = 0, h = 0;
     for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
@@ -181,13 +189,23 @@ void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* p
     if (n) k_store_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, vel, n, pos3, vel3);
 }
 
-void launch_hash_count(const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts, uint2* key_slot,
-                       cudaStream_t s) {
-    if (n) k_hash_count<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, counts, key_slot);
+void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,
+                       uint2* key_slot, cudaStream_t s) {
+    if (!n) return;
+    if (d.table)
+        k_hash_count<true><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, d.table, d.scene_off, d.nscenes, counts,
+                                                                  key_slot);
+    else
+        k_hash_count<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, counts, key_slot);
 }
 
-void launch_keys(const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys, cudaStream_t s) {
-    if (n) k_keys<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, keys);
+void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
+                 cudaStream_t s) {
+    if (!n) return;
+    if (d.table)
+        k_keys<true><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, d.table, d.scene_off, d.nscenes, keys);
+    else
+        k_keys<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, keys);
 }
 
 static void launch_scan_reduce(DeviceState& d, cudaStream_t s) {
@@ -223,8 +241,15 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
                             cudaStream_t s) {
     if (!d.n) return;
     with_reach(c.reach, [&](auto R) {
-        k_neighbour_stats<decltype(R)::value>
-            <<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, count, hash);
+        constexpr int K = decltype(R)::value;
+        if (d.table) {
+            if constexpr (K <= 2)
+                k_neighbour_stats<K, true><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(
+                    d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, count, hash);
+        } else {
+            k_neighbour_stats<K, false>
+                <<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.cell_start, d.n, c, nullptr, nullptr, 0, count, hash);
+        }
     });
 }
 

@@ -32,6 +32,7 @@ struct SimConst {
     float cell_w[3];
     float prune_margin;
     float prune_h2;
+    uint32_t cell_base;   // first key of this scene's cells (0 outside a batch)
 };
 
 // Fill `c` from `p`; returns SF_OK or an error code (with message in `why`).
@@ -39,6 +40,10 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why);
 
 // Scene generator (sf_scenes.cpp): AoS float3 positions of `scene`.
 int scene_points(const sf_params& p, int scene, uint64_t seed, std::vector<float>& out, const char** why);
+// Batched cube workload (sf_scenes.cpp): per-scene parameters, counts and the
+// concatenated AoS float3 positions.
+int batch_cubes(uint64_t seed, uint32_t nscenes, const sf_params& base, std::vector<sf_params>& params,
+                std::vector<uint32_t>& counts, std::vector<float>& pos, const char** why);
 
 // Kernel choices of a context (all give bit-identical results).
 struct Tuning {
@@ -70,6 +75,11 @@ struct DeviceState {
     uint32_t* cell_start = nullptr;  // ncells + 1
     uint32_t* tile_sums = nullptr;   // one per scan tile
     uint32_t ntiles = 0;
+    // batches of independent scenes (null for a single scene): per-scene
+    // constants and the first particle index of each scene (nscenes + 1)
+    const SimConst* table = nullptr;
+    const uint32_t* scene_off = nullptr;
+    uint32_t nscenes = 0;
 };
 
 // Neighbour lists: up to kNbCap neighbours per particle, in tiles of kNbTile
@@ -86,8 +96,8 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 // ---- kernel launchers (sf_kernels.cu); all enqueue on `s` ---------------
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s);
-void launch_hash_count(const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts, uint2* key_slot,
-                       cudaStream_t s);
+void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,
+                       uint2* key_slot, cudaStream_t s);
 void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
                     cudaStream_t s);
@@ -98,7 +108,8 @@ void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
 void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s);
 // forces only: acceleration into d.accel (inspection)
 void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s);
-void launch_keys(const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys, cudaStream_t s);
+void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
+                 cudaStream_t s);
 void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
                             cudaStream_t s);
 

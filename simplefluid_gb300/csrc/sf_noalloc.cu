@@ -134,7 +134,7 @@ int noalloc_density(const sf_params& p, const SimConst& c, const float* d_pos_xy
         return SF_ERR_CUDA;
     }
     launch_load_aos(d_pos_xyz, nullptr, n, d.pos2, d.vel2, stream);
-    launch_hash_count(d.pos2, n, c, d.counts, d.key_slot, stream);
+    launch_hash_count(d, d.pos2, n, c, d.counts, d.key_slot, stream);
     enqueue_sort_tail(d, stream);
     launch_density(d, c, stream);
     k_density_to_caller_order<<<(n + 255) / 256, 256, 0, stream>>>(d.pos, d.rho, d.pr, n, d_rho, d_pressure);

@@ -172,6 +172,52 @@ int build_scene(const sf_params& p, int scene, uint64_t seed, Points& out, const
 
 }  // namespace
 
+// Batched cube workload: scene s draws, in order from std::mt19937_64(seed),
+// u_n, u_mu, u_k (each (draw >> 11) * 2^-53): particle count
+// N_s = round(exp(ln 2000 + u_n (ln 65536 - ln 2000))) clamped to [2000, 65536],
+// viscosity 0.005 + 0.045 u_mu, stiffness 20 + 80 u_k.  The scene is a lattice
+// of spacing 2r with m = ceil(cbrt(N_s)) points per side (x outer, z inner; the
+// first N_s points), anchored at m*r + r so the block sits centred in its box
+// [0, 4 m r]^3, and drops under gravity.  Other parameters come from `base`.
+int batch_cubes(uint64_t seed, uint32_t nscenes, const sf_params& base, std::vector<sf_params>& params,
+                std::vector<uint32_t>& counts, std::vector<float>& pos, const char** why) {
+    if (!(base.particle_radius > 0.f)) {
+        *why = "particle_radius must be positive";
+        return SF_ERR_INVALID_ARGUMENT;
+    }
+    std::mt19937_64 eng(seed);
+    auto uni = [&eng]() { return (double)(eng() >> 11) * (1.0 / 9007199254740992.0); };
+    params.assign(nscenes, base);
+    counts.assign(nscenes, 0);
+    pos.clear();
+    const float r = base.particle_radius, spacing = 2.0f * r;
+    for (uint32_t s = 0; s < nscenes; ++s) {
+        const double un = uni(), umu = uni(), uk = uni();
+        double nd = std::exp(std::log(2000.0) + un * (std::log(65536.0) - std::log(2000.0)));
+        uint32_t n = (uint32_t)std::llround(nd);
+        n = n < 2000 ? 2000 : (n > 65536 ? 65536 : n);
+        uint32_t m = 1;
+        while ((uint64_t)m * m * m < n) ++m;
+        sf_params& p = params[s];
+        p.viscosity = (float)(0.005 + 0.045 * umu);
+        p.pressure_stiffness = (float)(20.0 + 80.0 * uk);
+        p.scene = SF_SCENE_CUBE_DROP;
+        const float ext = 4.0f * (float)m * r;
+        for (int a = 0; a < 3; ++a) {
+            p.box_min[a] = 0.0f;
+            p.box_max[a] = ext;
+        }
+        const float origin = (float)m * r + r;
+        uint32_t emitted = 0;
+        for (uint32_t i = 0; i < m && emitted < n; ++i)
+            for (uint32_t j = 0; j < m && emitted < n; ++j)
+                for (uint32_t k = 0; k < m && emitted < n; ++k, ++emitted)
+                    emit(pos, origin + spacing * (float)i, origin + spacing * (float)j, origin + spacing * (float)k);
+        counts[s] = n;
+    }
+    return SF_OK;
+}
+
 int scene_points(const sf_params& p, int scene, uint64_t seed, std::vector<float>& out, const char** why) {
     return build_scene(p, scene, seed, out, why);
 }

@@ -373,3 +373,105 @@ class Simulator:
             self.particleChanged()
         if self.numParticleChanged:
             self.numParticleChanged(self.m_SPHSolver.getNumParticles())
+
+
+def batch_cubes(seed: int, nscenes: int, base: SPHParameters):
+    """The batched-cube workload: (per-scene sf_params list, counts, concatenated positions)."""
+    lib = C.load()
+    bp = base.to_c()
+    total = ctypes.c_uint64()
+    C.check(lib.sf_batch_cubes(seed, nscenes, byref(bp), None, None, None, 0, byref(total)))
+    params = (C.sf_params * nscenes)()
+    counts = np.empty(nscenes, np.uint32)
+    pos = np.empty((total.value, 3), np.float32)
+    C.check(lib.sf_batch_cubes(seed, nscenes, byref(bp), params, _vp(counts), _vp(pos), total.value, byref(total)))
+    return list(params), counts, pos
+
+
+class SPHBatch:
+    """Many independent scenes advanced together (one graph launch per step)."""
+
+    def __init__(self, scene_params):
+        self._lib = C.load()
+        n = len(scene_params)
+        arr = (C.sf_params * n)()
+        for s, p in enumerate(scene_params):
+            arr[s] = p.to_c() if isinstance(p, SPHParameters) else p
+        self._b = c_void_p()
+        C.check(self._lib.sf_batch_create(arr, n, byref(self._b)))
+        self.nscenes = n
+
+    def close(self):
+        if self._b:
+            self._lib.sf_batch_destroy(self._b)
+            self._b = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._b
+
+    def setState(self, counts, pos, vel=None):
+        counts = np.ascontiguousarray(counts, np.uint32)
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        if counts.size != self.nscenes or int(counts.sum()) != pos.shape[0]:
+            raise ValueError("counts must have one entry per scene and sum to the number of particles")
+        C.check(self._lib.sf_batch_set_state(self._b, _vp(counts), _vp(pos), _vp(vel)))
+
+    def numParticles(self) -> int:
+        n = c_uint32()
+        C.check(self._lib.sf_batch_num_particles(self._b, byref(n)))
+        return n.value
+
+    def getState(self):
+        n = self.numParticles()
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        C.check(self._lib.sf_batch_get_state(self._b, _vp(pos), _vp(vel), n))
+        return pos, vel
+
+    def getParams(self, scene: int) -> C.sf_params:
+        p = C.sf_params()
+        C.check(self._lib.sf_batch_get_params(self._b, scene, byref(p)))
+        return p
+
+    def step(self, nsteps: int):
+        C.check(self._lib.sf_batch_step(self._b, int(nsteps)))
+
+    def synchronize(self):
+        C.check(self._lib.sf_batch_synchronize(self._b))
+
+    def setCellsPerH(self, k: int):
+        C.check(self._lib.sf_batch_set_cells_per_h(self._b, int(k)))
+
+    def setTuning(self, t: C.sf_tuning):
+        C.check(self._lib.sf_batch_set_tuning(self._b, byref(t)))
+
+    def getTuning(self) -> C.sf_tuning:
+        t = C.sf_tuning()
+        C.check(self._lib.sf_batch_get_tuning(self._b, byref(t)))
+        return t
+
+    def autotune(self, trial_steps: int = 10):
+        t = C.sf_tuning()
+        k = ctypes.c_int32()
+        ms = c_float()
+        C.check(self._lib.sf_batch_autotune(self._b, int(trial_steps), byref(t), byref(k), byref(ms)))
+        return t, k.value, ms.value
+
+    def timedSteps(self, nsteps: int, flush_bytes: int = 0) -> float:
+        ms = c_float()
+        C.check(self._lib.sf_batch_step_timed(self._b, int(nsteps), int(flush_bytes), byref(ms), None))
+        return ms.value

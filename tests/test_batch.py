@@ -1,0 +1,112 @@
+"""Batches of independent scenes: the workload generator (CPU) and the batched
+step (GPU) against the oracle and against per-scene contexts."""
+import numpy as np
+import pytest
+
+from helpers import params_16k
+from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes
+from simplefluid_gb300 import _capi as C
+
+
+def small_base(**kw):
+    base = dict(particleRadius=0.01, kernelRadius=0.04)
+    base.update(kw)
+    return SPHParameters(**base)
+
+
+def test_batch_cubes_workload_definition():
+    params, counts, pos = batch_cubes(20171, 256, small_base())
+    assert len(params) == 256 and counts.size == 256
+    assert counts.min() >= 2000 and counts.max() <= 65536
+    assert pos.shape[0] == int(counts.sum())
+    assert 3.5e6 < counts.sum() < 6.5e6  # log-uniform mean ~ 18.2k per scene
+    mus = np.array([p.viscosity for p in params])
+    ks = np.array([p.pressure_stiffness for p in params])
+    assert mus.min() >= 0.005 and mus.max() <= 0.05 and ks.min() >= 20 and ks.max() <= 100
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    for s in (0, 17, 255):
+        blk = pos[off[s]:off[s + 1]]
+        hi = params[s].box_max[0]
+        assert np.all(blk > 0) and np.all(blk < hi)
+    p2, c2, pos2 = batch_cubes(20171, 256, small_base())
+    assert np.array_equal(c2, counts) and np.array_equal(pos2.view(np.uint32), pos.view(np.uint32))
+    _, c3, _ = batch_cubes(7, 256, small_base())
+    assert not np.array_equal(c3, counts)
+
+
+def _scene_slices(counts):
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return [slice(int(off[s]), int(off[s + 1])) for s in range(len(counts))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [1, 2])
+def test_batch_matches_oracle_per_scene(oracle, K):
+    params, counts, pos = batch_cubes(5, 6, small_base(cellsPerH=K))
+    rng = np.random.default_rng(5)
+    vel = rng.normal(scale=0.1, size=pos.shape).astype(np.float32)
+    with SPHBatch(params) as b:
+        b.setState(counts, pos, vel)
+        b.step(15)
+        gpos, gvel = b.getState()
+        for s in range(len(params)):
+            assert b.getParams(s).cells_per_h == K
+    for s, sl in enumerate(_scene_slices(counts)):
+        st = oracle.State(pos[sl], vel[sl])
+        st.step(params[s], 15)
+        st.sort(params[s])
+        opos, ovel = st.original_order()
+        assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
+        assert np.array_equal(gvel[sl].view(np.uint32), ovel.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+def test_batch_equals_per_scene_contexts():
+    params, counts, pos = batch_cubes(11, 5, small_base())
+    with SPHBatch(params) as b:
+        b.setState(counts, pos)
+        b.step(25)
+        gpos, _ = b.getState()
+    for s, sl in enumerate(_scene_slices(counts)):
+        with SPHSolver(SPHParameters.from_c(params[s])) as ctx:
+            ctx.setParticles(pos[sl])
+            ctx.step(25)
+            spos = ctx.getParticles()
+        assert np.array_equal(gpos[sl].view(np.uint32), spos.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+def test_batch_autotune_restores_state_and_choice_is_valid(oracle):
+    params, counts, pos = batch_cubes(3, 4, small_base())
+    with SPHBatch(params) as b:
+        b.setState(counts, pos)
+        b.step(3)
+        before = b.getState()
+        t, K, ms = b.autotune(trial_steps=3)
+        after = b.getState()
+        assert K in (1, 2) and ms > 0
+        assert t.list_mode in (C.SF_LIST_TILE_STAGED, C.SF_LIST_TILE) and t.prefetch == 2
+        assert np.array_equal(before[0].view(np.uint32), after[0].view(np.uint32))
+        got = b.getTuning()
+        assert bytes(got) == bytes(t)
+        b.step(5)
+        gpos, _ = b.getState()
+    # the chosen configuration still matches the oracle (with the chosen K)
+    for s, sl in enumerate(_scene_slices(counts)):
+        p = params[s]
+        p.cells_per_h = K
+        st = oracle.State(before[0][sl], before[1][sl])
+        st.step(p, 5)
+        st.sort(p)
+        opos, _ = st.original_order()
+        assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+def test_batch_rejects_mixed_grids():
+    a = small_base(cellsPerH=1).to_c()
+    b = small_base(cellsPerH=2).to_c()
+    with pytest.raises(C.SFError):
+        SPHBatch([a, b])
+    with pytest.raises(C.SFError):
+        SPHBatch([small_base(cellsPerH=3).to_c()])
