@@ -208,6 +208,28 @@ SF_API const char* sf_stage_name(uint32_t stage);
 SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
                                   uint32_t nstages);
 
+/* ---- differentiation -------------------------------------------------------
+ * Not in the reference.  A hand-written adjoint of the sub-step (density, EOS,
+ * forces, integration and box), with each step's neighbour structure held
+ * fixed.  sf_forward advances like sf_step and records checkpoints of the
+ * state every `ckpt_every` steps; sf_adjoint re-runs each segment forward from
+ * its checkpoint (recomputing neighbour lists and states) and propagates the
+ * given adjoint of the final state back to the state at the sf_forward call,
+ * plus the gradients with respect to viscosity and stiffness.  Memory is the
+ * checkpoints (32 B per particle each) plus one segment of step records.
+ * All arrays are host AoS float3 in the caller's particle order; inputs may be
+ * NULL (zero), outputs may be NULL (not returned).  The particle state after
+ * sf_adjoint is the state sf_forward ended with. */
+SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every);
+SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dloss_dv, float* dloss_dx0,
+                            float* dloss_dv0, float* dloss_dviscosity, float* dloss_dstiffness);
+/* Loss = sum over res^3 cells of (H_c - target_c)^2, H the cloud-in-cell
+ * histogram of the current positions on cell-centred bins over the box,
+ * normalised by the particle count (accumulated in 2^-32 fixed point, so it
+ * does not depend on summation order; the loss is returned in double);
+ * dloss_dx (may be NULL) receives dL/dx. */
+SF_API sf_status sf_loss_histogram(sf_ctx* ctx, const float* target, uint32_t res, double* loss_out, float* dloss_dx);
+
 /* ---- batches of independent scenes -------------------------------------
  * Not in the reference (which runs one scene): many independent scenes of
  * uneven size, each with its own parameters and box, advanced together — one

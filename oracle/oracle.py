@@ -58,6 +58,15 @@ def lib() -> ctypes.CDLL:
             getattr(l, f"sfo_integrate_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p]
             getattr(l, f"sfo_neighbour_stats_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
             getattr(l, f"sfo_step_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_uint32, c_int]
+        for sfx in ("f32", "f64"):
+            getattr(l, f"sfo_grad_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p,
+                                                      c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                      c_void_p, c_int]
+            getattr(l, f"sfo_adjoint_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_uint32,
+                                                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                         c_void_p, c_int]
+            getattr(l, f"sfo_loss_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
+                                                      c_void_p]
         l.sfo_max_threads.argtypes = []
         _lib = l
     return _lib
@@ -172,6 +181,56 @@ class State:
         inv = np.empty_like(self.ids)
         inv[self.ids] = np.arange(self.n, dtype=np.uint32)
         return self.pos[inv], self.vel[inv]
+
+
+def grad(p: sf_params, pos0, vel0, nsteps: int, target, ckpt: int = 20, dtype=np.float64, threads: int = 0):
+    """Forward + CIC loss + adjoint: (loss, dL/dx0, dL/dv0, dL/dmu, dL/dk, final positions)."""
+    dt = np.dtype(dtype)
+    sfx = "f32" if dt == np.float32 else "f64"
+    pos0 = np.ascontiguousarray(pos0, dt).reshape(-1, 3)
+    vel0 = np.ascontiguousarray(vel0, dt).reshape(-1, 3)
+    tgt = np.ascontiguousarray(target, dt).ravel()
+    res = int(round(tgt.size ** (1 / 3)))
+    n = pos0.shape[0]
+    loss = np.zeros(1, dt)
+    gx, gv, pf = np.zeros_like(pos0), np.zeros_like(vel0), np.zeros_like(pos0)
+    gm, gk = np.zeros(1, dt), np.zeros(1, dt)
+    _chk(getattr(lib(), f"sfo_grad_{sfx}")(ctypes.byref(p), n, _ptr(pos0), _ptr(vel0), nsteps, ckpt, _ptr(tgt), res,
+                                           _ptr(loss), _ptr(gx), _ptr(gv), _ptr(gm), _ptr(gk), _ptr(pf), threads),
+         "grad")
+    return float(loss[0]), gx, gv, float(gm[0]), float(gk[0]), pf
+
+
+def adjoint(p: sf_params, pos0, vel0, nsteps: int, seed_x, seed_v=None, ckpt: int = 20, dtype=np.float64,
+            threads: int = 0):
+    """Adjoint of `nsteps` from the given final-state adjoint: (dx0, dv0, dmu, dk, final positions)."""
+    dt = np.dtype(dtype)
+    sfx = "f32" if dt == np.float32 else "f64"
+    pos0 = np.ascontiguousarray(pos0, dt).reshape(-1, 3)
+    vel0 = np.ascontiguousarray(vel0, dt).reshape(-1, 3)
+    sx = np.ascontiguousarray(seed_x, dt).reshape(-1, 3)
+    sv = None if seed_v is None else np.ascontiguousarray(seed_v, dt).reshape(-1, 3)
+    n = pos0.shape[0]
+    gx, gv, pf = np.zeros_like(pos0), np.zeros_like(vel0), np.zeros_like(pos0)
+    gm, gk = np.zeros(1, dt), np.zeros(1, dt)
+    _chk(getattr(lib(), f"sfo_adjoint_{sfx}")(ctypes.byref(p), n, _ptr(pos0), _ptr(vel0), nsteps, ckpt, _ptr(sx),
+                                              _ptr(sv), _ptr(gx), _ptr(gv), _ptr(gm), _ptr(gk), _ptr(pf), threads),
+         "adjoint")
+    return gx, gv, float(gm[0]), float(gk[0]), pf
+
+
+def loss(p: sf_params, pos, target, dtype=np.float64):
+    """CIC histogram loss and dL/dx of positions (n x 3)."""
+    dt = np.dtype(dtype)
+    sfx = "f32" if dt == np.float32 else "f64"
+    pos = np.ascontiguousarray(pos, dt).reshape(-1, 3)
+    tgt = np.ascontiguousarray(target, dt).ravel()
+    res = int(round(tgt.size ** (1 / 3)))
+    out = np.zeros(1, dt)
+    g = np.zeros_like(pos)
+    _chk(getattr(lib(), f"sfo_loss_{sfx}")(ctypes.byref(p), pos.shape[0], _ptr(pos), _ptr(tgt), res, _ptr(out),
+                                           _ptr(g), None), "loss")
+    return float(out[0]), g
 
 
 def max_threads() -> int:

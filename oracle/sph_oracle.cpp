@@ -244,7 +244,8 @@ void density_pass(const Derived<Real>& d, uint32_t n, const Real* pos, const std
 
 template <typename Real>
 void accel_pass(const Derived<Real>& d, uint32_t n, const Real* pos, const Real* vel, const Real* prs,
-                const Real* inv_rho, const std::vector<uint32_t>& cs, Real* acc) {
+                const Real* inv_rho, const std::vector<uint32_t>& cs, Real* acc, Real* ap_out = nullptr,
+                Real* av_out = nullptr) {
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
         const Real* xi = pos + 3 * i;
@@ -274,6 +275,8 @@ void accel_pass(const Derived<Real>& d, uint32_t n, const Real* pos, const Real*
         for (int a = 0; a < 3; ++a) {
             const Real t = std::fma(d.cp, ap[a], d.cv * av[a]);
             acc[3 * i + a] = std::fma(t, inv_rho[i], d.g[a]);
+            if (ap_out) ap_out[3 * i + a] = ap[a];
+            if (av_out) av_out[3 * i + a] = av[a];
         }
     }
 }
@@ -316,6 +319,330 @@ int step_impl(const sf_params* p, uint32_t n, Real* pos, Real* vel, uint32_t* id
         accel_pass(d, n, pos, vel, prs.data(), inv_rho.data(), cs, acc.data());
         integrate_pass(d, n, pos, vel, acc.data());
     }
+    return SF_OK;
+}
+
+
+// ------------------------------------------------------------- adjoint --
+// Hand-written adjoint of one sub-step with the neighbour structure of that
+// step held fixed (piecewise-constant), and of the CIC histogram loss.  The
+// CUDA adjoint performs the same operations in the same order.
+//
+// Forward step per particle (sorted order of the step), for reference:
+//   rho = cd sum_j (h^2 - r^2)^3, p = EOS(rho) (clamped), inv = 1/rho
+//   AP = sum_j (p_i + p_j) w_ij (hr/r) d_ij,  AV = sum_j w_ij (v_j - v_i),
+//   w_ij = hr inv_j, hr = h - r, d_ij = x_i - x_j
+//   a = (cp AP + cv AV) inv + g;  v' = v + dt a;  x' = x + dt v';  box clamp.
+template <typename Real>
+struct StepRecord {
+    std::vector<Real> pos, vel, rho, prs, inv, ap, av;
+    std::vector<uint32_t> ids, cs;
+};
+
+template <typename Real>
+inline Real dot3(const Real* a, const Real* b) {
+    return std::fma(a[2], b[2], std::fma(a[1], b[1], a[0] * b[0]));
+}
+
+// dp/drho and dp/dk of the equation of state, 0 where the clamp is active.
+template <typename Real>
+inline void eos_derivs(const Derived<Real>& d, Real rho, Real* dpdrho, Real* dpdk) {
+    Real ppre, dr, dk;
+    if (d.eos == SF_EOS_TAIT) {
+        const Real x = rho * d.inv_rho0;
+        const Real x2 = x * x;
+        const Real x4 = x2 * x2;
+        const Real x6 = x4 * x2;
+        const Real x7 = x6 * x;
+        ppre = d.k * (x7 - (Real)1);
+        dr = ((Real)7 * d.k) * (x6 * d.inv_rho0);
+        dk = x7 - (Real)1;
+    } else {
+        ppre = d.k * (rho - d.rho0);
+        dr = d.k;
+        dk = rho - d.rho0;
+    }
+    const bool act = d.attractive || ppre > (Real)0;
+    *dpdrho = act ? dr : (Real)0;
+    *dpdk = act ? dk : (Real)0;
+}
+
+template <typename Real>
+void adjoint_step(const Derived<Real>& d, uint32_t n, const StepRecord<Real>& R, Real* Xb, Real* Vb, double* mub,
+                  double* kb) {
+    std::vector<Real> apb(3 * (size_t)n), avb(3 * (size_t)n), invb(n), xdir(3 * (size_t)n), vdir(3 * (size_t)n);
+    std::vector<Real> cvb(n), rhob(n), xf(3 * (size_t)n), vf(3 * (size_t)n), kbp(n);
+    // P1: integration and the acceleration's own inputs
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const uint32_t id = R.ids[i];
+        const Real inv = R.inv[i];
+        Real tb[3], t[3], ab3[3];
+        for (int a = 0; a < 3; ++a) {
+            const Real x = R.pos[3 * i + a], v = R.vel[3 * i + a];
+            t[a] = std::fma(d.cp, R.ap[3 * i + a], d.cv * R.av[3 * i + a]);
+            const Real acc = std::fma(t[a], inv, d.g[a]);
+            const Real vpre = std::fma(d.dt, acc, v);
+            const Real xpre = std::fma(d.dt, vpre, x);
+            const bool lo = xpre < d.lo[a], hi = xpre > d.hi[a];
+            const bool pass = !lo && !hi;
+            const Real sv = ((lo && vpre < (Real)0) || (hi && vpre > (Real)0)) ? -d.e : (Real)1;
+            const Real xbpre = pass ? Xb[3 * (size_t)id + a] : (Real)0;
+            const Real vbpre = std::fma(sv, Vb[3 * (size_t)id + a], d.dt * xbpre);
+            xdir[3 * i + a] = xbpre;
+            vdir[3 * i + a] = vbpre;
+            ab3[a] = d.dt * vbpre;
+            tb[a] = ab3[a] * inv;
+            apb[3 * i + a] = d.cp * tb[a];
+            avb[3 * i + a] = d.cv * tb[a];
+        }
+        invb[i] = dot3(ab3, t);
+        const Real av3[3] = {R.av[3 * i], R.av[3 * i + 1], R.av[3 * i + 2]};
+        cvb[i] = dot3(tb, av3);
+    }
+    // P2: pair terms of the forces, both orientations of each pair; then the
+    // density adjoint of each particle (inverse and equation of state)
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t k = 0; k < (int64_t)n; ++k) {
+        const Real* xk = &R.pos[3 * k];
+        const Real* vk = &R.vel[3 * k];
+        const Real pk = R.prs[k], invk = R.inv[k];
+        const Real* apbk = &apb[3 * k];
+        const Real* avbk = &avb[3 * k];
+        Real pb = 0, invacc = 0, xb[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+        for_candidates(d, R.cs, xk, [&](uint32_t j) {
+            if ((int64_t)j == k) return;
+            Real dd[3];
+            const Real r2 = r2_of(xk, &R.pos[3 * (size_t)j], dd);
+            if (!(r2 < d.h2)) return;
+            const Real r = std::sqrt(r2);
+            const Real hr = d.h - r;
+            const Real pj = R.prs[j], invj = R.inv[j];
+            const Real* vj = &R.vel[3 * (size_t)j];
+            const Real* apbj = &apb[3 * (size_t)j];
+            const Real* avbj = &avb[3 * (size_t)j];
+            const Real dv[3] = {vj[0] - vk[0], vj[1] - vk[1], vj[2] - vk[2]};
+            const Real ps = pk + pj;
+            // orientation A: k is i, j is the neighbour
+            const Real wkj = hr * invj;
+            for (int a = 0; a < 3; ++a) vb[a] = std::fma(-wkj, avbk[a], vb[a]);
+            Real wb = dot3(avbk, dv);
+            Real rb = 0;
+            // orientation B: j is i, k is the neighbour
+            const Real wjk = hr * invk;
+            for (int a = 0; a < 3; ++a) vb[a] = std::fma(wjk, avbj[a], vb[a]);
+            Real wb2 = -dot3(avbj, dv);
+            Real rb2 = 0;
+            if (r > (Real)0) {
+                const Real q = hr / r;
+                const Real S = (ps * wkj) * q;
+                const Real Sb = dot3(apbk, dd);
+                for (int a = 0; a < 3; ++a) xb[a] = std::fma(S, apbk[a], xb[a]);
+                pb = std::fma(Sb, wkj * q, pb);
+                wb = std::fma(Sb, ps * q, wb);
+                const Real qb = Sb * (ps * wkj);
+                rb = -((qb * d.h) / r2);
+                const Real S2 = (ps * wjk) * q;
+                const Real Sb2 = -dot3(apbj, dd);
+                for (int a = 0; a < 3; ++a) xb[a] = std::fma(-S2, apbj[a], xb[a]);
+                pb = std::fma(Sb2, wjk * q, pb);
+                wb2 = std::fma(Sb2, ps * q, wb2);
+                const Real qb2 = Sb2 * (ps * wjk);
+                rb2 = -((qb2 * d.h) / r2);
+            }
+            rb = std::fma(-wb, invj, rb);
+            invacc = std::fma(wb2, hr, invacc);
+            rb2 = std::fma(-wb2, invk, rb2);
+            if (r > (Real)0) {
+                const Real g = (rb + rb2) / r;
+                for (int a = 0; a < 3; ++a) xb[a] = std::fma(g, dd[a], xb[a]);
+            }
+        });
+        const Real ib = invb[k] + invacc;
+        Real dpdrho, dpdk;
+        eos_derivs(d, R.rho[k], &dpdrho, &dpdk);
+        rhob[k] = std::fma(pb, dpdrho, -((ib * invk) * invk));
+        kbp[k] = pb * dpdk;
+        for (int a = 0; a < 3; ++a) {
+            xf[3 * k + a] = xb[a];
+            vf[3 * k + a] = vb[a];
+        }
+    }
+    // P4: density adjoint onto positions; write the step's input adjoints
+    const Real m6cd = (Real)(-6.0 * (double)d.cd);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t k = 0; k < (int64_t)n; ++k) {
+        const Real* xk = &R.pos[3 * k];
+        const Real rbk = rhob[k];
+        Real xd[3] = {0, 0, 0};
+        for_candidates(d, R.cs, xk, [&](uint32_t j) {
+            if ((int64_t)j == k) return;
+            Real dd[3];
+            const Real r2 = r2_of(xk, &R.pos[3 * (size_t)j], dd);
+            if (!(r2 < d.h2)) return;
+            const Real q = d.h2 - r2;
+            const Real sc = (rbk + rhob[j]) * (q * q);
+            for (int a = 0; a < 3; ++a) xd[a] = std::fma(sc, dd[a], xd[a]);
+        });
+        const uint32_t id = R.ids[k];
+        for (int a = 0; a < 3; ++a) {
+            const Real xt = xdir[3 * k + a] + xf[3 * k + a];
+            Xb[3 * (size_t)id + a] = std::fma(m6cd, xd[a], xt);
+            Vb[3 * (size_t)id + a] = vdir[3 * k + a] + vf[3 * k + a];
+        }
+    }
+    double cvs = 0, ks = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        cvs += (double)cvb[i];
+        ks += (double)kbp[i];
+    }
+    *mub += cvs;
+    *kb += ks;
+}
+
+// CIC histogram on res^3 cells over the box (cell-centred), normalised by n.
+template <typename Real>
+void hist_weights(const Derived<Real>& d, const Real* bext, uint32_t res, const Real* x, int i0[3], Real w0[3],
+                  Real w1[3], Real dw[3]) {
+    for (int a = 0; a < 3; ++a) {
+        const Real inv = (Real)res / bext[a];
+        const Real u = (x[a] - d.bmin[a]) * inv - (Real)0.5;
+        const Real fl = std::floor(u);
+        const Real f = u - fl;
+        i0[a] = (int)fl;
+        w0[a] = (Real)1 - f;
+        w1[a] = f;
+        dw[a] = inv;
+    }
+}
+
+template <typename Real>
+Real histogram_loss(const Derived<Real>& d, const Real* bext, uint32_t n, const Real* pos, const Real* target,
+                    uint32_t res, Real* dldx, std::vector<double>* hist_out) {
+    const size_t nc = (size_t)res * res * res;
+    std::vector<double> H(nc, 0.0);
+    for (uint32_t p = 0; p < n; ++p) {
+        int i0[3];
+        Real w0[3], w1[3], dw[3];
+        hist_weights(d, bext, res, pos + 3 * (size_t)p, i0, w0, w1, dw);
+        for (int c = 0; c < 8; ++c) {
+            const int ix = i0[0] + (c & 1), iy = i0[1] + ((c >> 1) & 1), iz = i0[2] + ((c >> 2) & 1);
+            if (ix < 0 || iy < 0 || iz < 0 || ix >= (int)res || iy >= (int)res || iz >= (int)res) continue;
+            const Real w = ((c & 1) ? w1[0] : w0[0]) * ((c & 2) ? w1[1] : w0[1]) * ((c & 4) ? w1[2] : w0[2]);
+            H[((size_t)iz * res + iy) * res + ix] += (double)w;
+        }
+    }
+    double L = 0;
+    for (size_t c = 0; c < nc; ++c) {
+        H[c] /= (double)n;
+        const double e = H[c] - (double)target[c];
+        L += e * e;
+    }
+    if (dldx) {
+        for (uint32_t p = 0; p < n; ++p) {
+            int i0[3];
+            Real w0[3], w1[3], dw[3];
+            hist_weights(d, bext, res, pos + 3 * (size_t)p, i0, w0, w1, dw);
+            Real g[3] = {0, 0, 0};
+            for (int c = 0; c < 8; ++c) {
+                const int ix = i0[0] + (c & 1), iy = i0[1] + ((c >> 1) & 1), iz = i0[2] + ((c >> 2) & 1);
+                if (ix < 0 || iy < 0 || iz < 0 || ix >= (int)res || iy >= (int)res || iz >= (int)res) continue;
+                const size_t cc = ((size_t)iz * res + iy) * res + ix;
+                const Real e2 = (Real)(2.0 * (H[cc] - (double)target[cc]) / (double)n);
+                const Real wx = (c & 1) ? w1[0] : w0[0], wy = (c & 2) ? w1[1] : w0[1], wz = (c & 4) ? w1[2] : w0[2];
+                const Real sx = (c & 1) ? dw[0] : -dw[0], sy = (c & 2) ? dw[1] : -dw[1], sz = (c & 4) ? dw[2] : -dw[2];
+                g[0] += e2 * (sx * (wy * wz));
+                g[1] += e2 * (sy * (wx * wz));
+                g[2] += e2 * (sz * (wx * wy));
+            }
+            for (int a = 0; a < 3; ++a) dldx[3 * (size_t)p + a] = g[a];
+        }
+    }
+    if (hist_out) *hist_out = H;
+    return (Real)L;
+}
+
+// Forward nsteps from (pos0, vel0), CIC loss at the end (or, with `seed_x`,
+// the given adjoint of the final state instead), and the adjoint back to the
+// initial state, recomputing segments of `ckpt` steps from checkpoints.
+template <typename Real>
+int grad_impl(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0, uint32_t nsteps, uint32_t ckpt,
+              const Real* target, uint32_t res, Real* loss_out, Real* gx0, Real* gv0, Real* gmu, Real* gk,
+              Real* pos_final, int threads, const Real* seed_x = nullptr, const Real* seed_v = nullptr) {
+    Derived<Real> d;
+    int st = derive(p, &d);
+    if (st) return st;
+    if (!pos0 || !vel0 || n == 0 || ckpt == 0) return SF_ERR_INVALID_ARGUMENT;
+    if (!seed_x && (!target || res == 0)) return SF_ERR_INVALID_ARGUMENT;
+    set_threads(threads);
+    Real bext[3];
+    for (int a = 0; a < 3; ++a) bext[a] = (Real)((double)p->box_max[a] - (double)p->box_min[a]);
+    const size_t n3 = 3 * (size_t)n;
+    std::vector<Real> pos(pos0, pos0 + n3), vel(vel0, vel0 + n3);
+    std::vector<uint32_t> ids(n);
+    for (uint32_t i = 0; i < n; ++i) ids[i] = i;
+    struct Ckpt {
+        std::vector<Real> pos, vel;
+        std::vector<uint32_t> ids;
+    };
+    std::vector<Ckpt> cks;
+    std::vector<uint32_t> keys, cs;
+    std::vector<Real> prs(n), inv(n), acc(n3);
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        if (s % ckpt == 0) cks.push_back({pos, vel, ids});
+        sort_and_grid(d, n, pos.data(), vel.data(), ids.data(), keys, cs);
+        density_pass(d, n, pos.data(), cs, (Real*)nullptr, prs.data(), inv.data());
+        accel_pass(d, n, pos.data(), vel.data(), prs.data(), inv.data(), cs, acc.data());
+        integrate_pass(d, n, pos.data(), vel.data(), acc.data());
+    }
+    // loss at the final state (array order = the last step's sorted order)
+    std::vector<Real> Xb(n3, (Real)0), Vb(n3, (Real)0);
+    if (seed_x) {
+        std::memcpy(Xb.data(), seed_x, n3 * sizeof(Real));
+        if (seed_v) std::memcpy(Vb.data(), seed_v, n3 * sizeof(Real));
+    } else {
+        std::vector<Real> dldx(n3);
+        const Real L = histogram_loss(d, bext, n, pos.data(), target, res, dldx.data(), nullptr);
+        if (loss_out) *loss_out = L;
+        for (uint32_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) Xb[3 * (size_t)ids[i] + a] = dldx[3 * (size_t)i + a];
+    }
+    if (pos_final)
+        for (uint32_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) pos_final[3 * (size_t)ids[i] + a] = pos[3 * (size_t)i + a];
+    double mub = 0, kb = 0;
+    for (int64_t seg = (int64_t)cks.size() - 1; seg >= 0; --seg) {
+        const uint32_t s0 = (uint32_t)seg * ckpt, s1 = std::min(nsteps, s0 + ckpt);
+        std::vector<StepRecord<Real>> recs(s1 - s0);
+        std::vector<Real> ps = cks[seg].pos, vs = cks[seg].vel;
+        std::vector<uint32_t> is = cks[seg].ids;
+        for (uint32_t s = s0; s < s1; ++s) {
+            StepRecord<Real>& R = recs[s - s0];
+            sort_and_grid(d, n, ps.data(), vs.data(), is.data(), keys, R.cs);
+            R.pos = ps;
+            R.vel = vs;
+            R.ids = is;
+            R.rho.resize(n);
+            R.prs.resize(n);
+            R.inv.resize(n);
+            R.ap.resize(n3);
+            R.av.resize(n3);
+            density_pass(d, n, ps.data(), R.cs, R.rho.data(), R.prs.data(), R.inv.data());
+            accel_pass(d, n, ps.data(), vs.data(), R.prs.data(), R.inv.data(), R.cs, acc.data(), R.ap.data(),
+                       R.av.data());
+            integrate_pass(d, n, ps.data(), vs.data(), acc.data());
+        }
+        for (int64_t s = (int64_t)s1 - 1; s >= (int64_t)s0; --s) adjoint_step(d, n, recs[s - s0], Xb.data(), Vb.data(), &mub, &kb);
+    }
+    if (gx0) std::memcpy(gx0, Xb.data(), n3 * sizeof(Real));
+    if (gv0) std::memcpy(gv0, Vb.data(), n3 * sizeof(Real));
+    // cv = mu * m * 45 / (pi h^6)
+    const double pi = 3.14159265358979323846;
+    const double hh = (double)p->kernel_radius, rr = (double)p->particle_radius;
+    const double mass = (double)p->rest_density * (2.0 * rr) * (2.0 * rr) * (2.0 * rr);
+    const double h6 = hh * hh * hh * hh * hh * hh;
+    if (gmu) *gmu = (Real)(mub * (mass * 45.0 / (pi * h6)));
+    if (gk) *gk = (Real)kb;
     return SF_OK;
 }
 
@@ -569,6 +896,42 @@ int sfo_scene(const sf_params* p, int scene, uint64_t seed, float* pos3, uint32_
 
 SFO_DEFINE(f32, float)
 SFO_DEFINE(f64, double)
+
+#define SFO_GRAD(SUFFIX, Real)                                                                                   \
+    int sfo_grad_##SUFFIX(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0, uint32_t nsteps,    \
+                          uint32_t ckpt, const Real* target, uint32_t res, Real* loss, Real* gx0, Real* gv0,      \
+                          Real* gmu, Real* gk, Real* pos_final, int threads) {                                   \
+        return grad_impl<Real>(p, n, pos0, vel0, nsteps, ckpt, target, res, loss, gx0, gv0, gmu, gk, pos_final,  \
+                               threads);                                                                         \
+    }                                                                                                            \
+    int sfo_loss_##SUFFIX(const sf_params* p, uint32_t n, const Real* pos, const Real* target, uint32_t res,      \
+                          Real* loss, Real* dldx, double* hist) {                                                \
+        Derived<Real> d;                                                                                         \
+        int st = derive(p, &d);                                                                                  \
+        if (st) return st;                                                                                       \
+        Real bext[3];                                                                                            \
+        for (int a = 0; a < 3; ++a) bext[a] = (Real)((double)p->box_max[a] - (double)p->box_min[a]);             \
+        std::vector<double> H;                                                                                   \
+        *loss = histogram_loss(d, bext, n, pos, target, res, dldx, hist ? &H : nullptr);                         \
+        if (hist) std::memcpy(hist, H.data(), H.size() * sizeof(double));                                        \
+        return SF_OK;                                                                                            \
+    }
+
+SFO_GRAD(f32, float)
+SFO_GRAD(f64, double)
+
+// Adjoint from a given final-state adjoint (seed_x, seed_v: n*3 in the
+// caller's particle order) — the same inputs sf_adjoint takes.
+#define SFO_ADJ(SUFFIX, Real)                                                                                     \
+    int sfo_adjoint_##SUFFIX(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0, uint32_t nsteps,  \
+                             uint32_t ckpt, const Real* seed_x, const Real* seed_v, Real* gx0, Real* gv0, Real* gmu, \
+                             Real* gk, Real* pos_final, int threads) {                                             \
+        if (!seed_x) return SF_ERR_INVALID_ARGUMENT;                                                               \
+        return grad_impl<Real>(p, n, pos0, vel0, nsteps, ckpt, nullptr, 0, nullptr, gx0, gv0, gmu, gk, pos_final,  \
+                               threads, seed_x, seed_v);                                                           \
+    }
+SFO_ADJ(f32, float)
+SFO_ADJ(f64, double)
 
 int sfo_max_threads(void) {
 #ifdef _OPENMP

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
 
 LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libsimplefluid_gb300.so")
@@ -115,6 +115,9 @@ PROTOTYPES = {
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
     "sf_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_forward": (c_int32, [c_void_p, c_uint32, c_uint32]),
+    "sf_adjoint": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, _P(c_float), _P(c_float)]),
+    "sf_loss_histogram": (c_int32, [c_void_p, c_void_p, c_uint32, _P(c_double), c_void_p]),
     "sf_batch_cubes": (c_int32, [c_uint64, c_uint32, _P(sf_params), c_void_p, c_void_p, c_void_p, c_uint64,
                                  _P(c_uint64)]),
     "sf_batch_create": (c_int32, [c_void_p, c_uint32, _P(c_void_p)]),

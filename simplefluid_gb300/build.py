@@ -29,6 +29,7 @@ SOURCES = [
     ("sf_grid.cu", ["-fmad=false"]),
     ("sf_density.cu", ["-fmad=false"]),
     ("sf_force.cu", ["-fmad=false"]),
+    ("sf_adjoint.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),

@@ -18,6 +18,33 @@
 
 #include "sf_internal.h"
 
+namespace sf {
+// Recorded trajectory of sf_forward and the adjoint's buffers.
+struct StepRec {
+    float4* pos = nullptr;
+    float4* vel = nullptr;
+    float2* pr = nullptr;
+    float* rho = nullptr;
+    uint32_t* nbr = nullptr;
+    uint32_t* cnt = nullptr;
+    uint32_t* cs = nullptr;
+    float4* sums = nullptr;
+};
+struct Trajectory {
+    uint32_t nsteps = 0, ckpt = 0, n = 0, ncells_pad = 0;
+    bool valid = false;
+    std::vector<float4*> ck;  // per checkpoint: pos then vel (2n float4)
+    std::vector<StepRec> rec; // ckpt steps of one segment
+    float4* snap = nullptr;   // 2n float4: the forward's final state
+    AdjointWork w;
+    uint32_t hist_res = 0;
+    unsigned long long* hist = nullptr;
+    float* e2 = nullptr;
+    float* target = nullptr;
+    double* hpartial = nullptr;
+};
+}  // namespace sf
+
 struct sf_ctx {
     sf_params params{};
     sf::SimConst c{};
@@ -28,6 +55,7 @@ struct sf_ctx {
     bool sorted = false;  // particles uploaded and cell-sorted
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
     size_t h_stage_bytes = 0;
+    sf::Trajectory* traj = nullptr;  // differentiable runs (sf_forward / sf_adjoint)
 };
 
 namespace {
@@ -128,6 +156,27 @@ void free_grid(sf::DeviceState& d) {
     if (d.tile_sums) cudaFree(d.tile_sums);
     d.counts = d.cell_start = d.tile_sums = nullptr;
     d.ncells = d.ncells_pad = d.ntiles = 0;
+}
+
+void free_rec(sf::StepRec& r) {
+    void* b[] = {r.pos, r.vel, r.pr, r.rho, r.nbr, r.cnt, r.cs, r.sums};
+    for (void* p : b)
+        if (p) cudaFree(p);
+    r = sf::StepRec{};
+}
+
+void free_trajectory(sf_ctx* ctx) {
+    sf::Trajectory* t = ctx->traj;
+    if (!t) return;
+    for (float4* p : t->ck)
+        if (p) cudaFree(p);
+    for (auto& r : t->rec) free_rec(r);
+    void* b[] = {t->snap, t->w.Xb, t->w.Vb, t->w.apb, t->w.avb, t->w.xdir, t->w.vdir, t->w.xf, t->w.vf,
+                 t->w.rhob, t->w.partial, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
+    for (void* p : b)
+        if (p) cudaFree(p);
+    delete t;
+    ctx->traj = nullptr;
 }
 
 void drop_graph(sf_ctx* ctx) {
@@ -423,6 +472,7 @@ SF_API sf_status sf_destroy(sf_ctx* ctx) {
     if (!ctx) return SF_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_trajectory(ctx);
     drop_graph(ctx);
     free_particles(ctx->d);
     free_grid(ctx->d);
@@ -1073,6 +1123,226 @@ SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning*
     if (chosen) *chosen = cands[best_i].t;
     if (chosen_cells_per_h) *chosen_cells_per_h = cands[best_i].K;
     if (chosen_ms_per_step) *chosen_ms_per_step = best / (float)trial_steps;
+    return SF_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- adjoint
+namespace {
+
+sf_status ensure_work(sf_ctx* ctx) {
+    sf::Trajectory* t = ctx->traj;
+    const size_t n = ctx->d.cap;
+    sf::AdjointWork& w = t->w;
+    if (w.Xb) return SF_OK;
+    SF_CUDA(cudaMalloc(&w.Xb, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.Vb, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.apb, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.avb, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.xdir, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.vdir, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.xf, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.vf, n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&w.rhob, n * sizeof(float)));
+    SF_CUDA(cudaMalloc(&w.partial, sf::adjoint_partial_count((uint32_t)n) * sizeof(double2)));
+    SF_CUDA(cudaMalloc(&w.scalars, 2 * sizeof(double)));
+    SF_CUDA(cudaMalloc(&t->snap, 2 * n * sizeof(float4)));
+    return SF_OK;
+}
+
+sf_status ensure_records(sf_ctx* ctx, uint32_t ckpt) {
+    sf::Trajectory* t = ctx->traj;
+    const size_t n = ctx->d.cap;
+    const size_t tiles = (n + sf::kNbTile - 1) / sf::kNbTile;
+    if (t->rec.size() == ckpt && t->ncells_pad == ctx->d.ncells_pad) return SF_OK;
+    for (auto& r : t->rec) free_rec(r);
+    t->rec.assign(ckpt, sf::StepRec{});
+    t->ncells_pad = ctx->d.ncells_pad;
+    for (auto& r : t->rec) {
+        SF_CUDA(cudaMalloc(&r.pos, n * sizeof(float4)));
+        SF_CUDA(cudaMalloc(&r.vel, n * sizeof(float4)));
+        SF_CUDA(cudaMalloc(&r.pr, n * sizeof(float2)));
+        SF_CUDA(cudaMalloc(&r.rho, n * sizeof(float)));
+        SF_CUDA(cudaMalloc(&r.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t)));
+        SF_CUDA(cudaMalloc(&r.cnt, n * sizeof(uint32_t)));
+        SF_CUDA(cudaMalloc(&r.cs, (size_t)ctx->d.ncells_pad * sizeof(uint32_t)));
+        SF_CUDA(cudaMalloc(&r.sums, 2 * n * sizeof(float4)));
+    }
+    return SF_OK;
+}
+
+// Put a sorted state (2n float4: pos then vel) back and rebuild the cell table.
+sf_status restore_sorted(sf_ctx* ctx, const float4* state) {
+    sf::DeviceState& d = ctx->d;
+    SF_CUDA(cudaMemcpyAsync(d.pos2, state, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    SF_CUDA(cudaMemcpyAsync(d.vel2, state + d.n, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
+    sf::enqueue_sort_tail(d, ctx->stream);
+    return check_launch("restore state");
+}
+
+sf_status upload_by_id(sf_ctx* ctx, float4* dst, const float* src_xyz) {
+    const uint32_t n = ctx->d.n;
+    std::vector<float4> h(n);
+    for (uint32_t i = 0; i < n; ++i)
+        h[i] = src_xyz ? make_float4(src_xyz[3 * (size_t)i], src_xyz[3 * (size_t)i + 1], src_xyz[3 * (size_t)i + 2], 0.f)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    SF_CUDA(cudaMemcpyAsync(dst, h.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+sf_status download_by_id(sf_ctx* ctx, float* dst_xyz, const float4* src) {
+    if (!dst_xyz) return SF_OK;
+    const uint32_t n = ctx->d.n;
+    std::vector<float4> h(n);
+    SF_TRY(copy_out(ctx, h.data(), src, (size_t)n * sizeof(float4)));
+    for (uint32_t i = 0; i < n; ++i) {
+        dst_xyz[3 * (size_t)i] = h[i].x;
+        dst_xyz[3 * (size_t)i + 1] = h[i].y;
+        dst_xyz[3 * (size_t)i + 2] = h[i].z;
+    }
+    return SF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every) {
+    SF_TRY(sf_make_ready(ctx));
+    if (ckpt_every == 0) return fail(SF_ERR_INVALID_ARGUMENT, "ckpt_every must be > 0");
+    if (!ctx->traj) ctx->traj = new sf::Trajectory();
+    sf::Trajectory* t = ctx->traj;
+    sf::DeviceState& d = ctx->d;
+    const uint32_t nck = (nsteps + ckpt_every - 1) / ckpt_every;
+    if (t->n != d.cap || t->ck.size() != nck) {
+        for (float4* p : t->ck)
+            if (p) cudaFree(p);
+        t->ck.assign(nck, nullptr);
+        for (auto& p : t->ck) SF_CUDA(cudaMalloc(&p, 2 * (size_t)d.cap * sizeof(float4)));
+    }
+    t->valid = false;
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        if (s % ckpt_every == 0) {
+            float4* c = t->ck[s / ckpt_every];
+            SF_CUDA(cudaMemcpyAsync(c, d.pos, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+            SF_CUDA(cudaMemcpyAsync(c + d.n, d.vel, (size_t)d.n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                    ctx->stream));
+        }
+        SF_CUDA(cudaGraphLaunch(ctx->step_graph, ctx->stream));
+    }
+    t->nsteps = nsteps;
+    t->ckpt = ckpt_every;
+    t->n = d.cap;
+    t->valid = true;
+    return SF_OK;
+}
+
+SF_API sf_status sf_loss_histogram(sf_ctx* ctx, const float* target, uint32_t res, double* loss_out, float* dloss_dx) {
+    SF_TRY(need_sorted(ctx));
+    if (!target || res == 0 || res > 1024 || !loss_out) return fail(SF_ERR_INVALID_ARGUMENT, "bad target or resolution");
+    SF_TRY(set_device(ctx));
+    if (!ctx->traj) ctx->traj = new sf::Trajectory();
+    sf::Trajectory* t = ctx->traj;
+    SF_TRY(ensure_work(ctx));
+    const size_t nc = (size_t)res * res * res;
+    if (t->hist_res != res) {
+        if (t->hist) cudaFree(t->hist);
+        if (t->e2) cudaFree(t->e2);
+        if (t->target) cudaFree(t->target);
+        if (t->hpartial) cudaFree(t->hpartial);
+        t->hist = nullptr;
+        t->e2 = t->target = nullptr;
+        t->hpartial = nullptr;
+        SF_CUDA(cudaMalloc(&t->hist, nc * sizeof(unsigned long long)));
+        SF_CUDA(cudaMalloc(&t->e2, nc * sizeof(float)));
+        SF_CUDA(cudaMalloc(&t->target, nc * sizeof(float)));
+        SF_CUDA(cudaMalloc(&t->hpartial, sf::histogram_partial_count(res) * sizeof(double)));
+        t->hist_res = res;
+    }
+    SF_TRY(copy_in(ctx, t->target, target, nc * sizeof(float)));
+    float ext[3];
+    for (int a = 0; a < 3; ++a) ext[a] = (float)((double)ctx->params.box_max[a] - (double)ctx->params.box_min[a]);
+    sf::launch_histogram_loss(ctx->d.pos, ctx->d.n, ctx->c, ext, res, t->target, t->hist, t->e2, t->hpartial, t->w.Xb,
+                              ctx->stream);
+    SF_TRY(check_launch("histogram loss"));
+    std::vector<double> part(sf::histogram_partial_count(res));
+    SF_TRY(copy_out(ctx, part.data(), t->hpartial, part.size() * sizeof(double)));
+    double L = 0.0;
+    for (double v : part) L += v;
+    *loss_out = L;
+    return download_by_id(ctx, dloss_dx, t->w.Xb);
+}
+
+SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dloss_dv, float* dloss_dx0,
+                            float* dloss_dv0, float* dloss_dviscosity, float* dloss_dstiffness) {
+    SF_TRY(need_sorted(ctx));
+    sf::Trajectory* t = ctx->traj;
+    if (!t || !t->valid || t->n != ctx->d.cap) return fail(SF_ERR_NOT_READY, "no recorded trajectory: call sf_forward");
+    SF_TRY(set_device(ctx));
+    SF_TRY(ensure_work(ctx));
+    SF_TRY(ensure_records(ctx, t->ckpt));
+    sf::DeviceState& d = ctx->d;
+    const uint32_t n = d.n;
+    sf::AdjointWork& w = t->w;
+    // keep the forward's final state to put back afterwards
+    SF_CUDA(cudaMemcpyAsync(t->snap, d.pos, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    SF_CUDA(cudaMemcpyAsync(t->snap + n, d.vel, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    SF_TRY(upload_by_id(ctx, w.Xb, dloss_dx));
+    SF_TRY(upload_by_id(ctx, w.Vb, dloss_dv));
+    SF_CUDA(cudaMemsetAsync(w.scalars, 0, 2 * sizeof(double), ctx->stream));
+    const uint32_t nck = (uint32_t)t->ck.size();
+    for (int64_t seg = (int64_t)nck - 1; seg >= 0; --seg) {
+        const uint32_t s0 = (uint32_t)seg * t->ckpt, s1 = std::min(t->nsteps, s0 + t->ckpt);
+        SF_TRY(restore_sorted(ctx, t->ck[seg]));
+        for (uint32_t s = s0; s < s1; ++s) {
+            sf::StepRec& r = t->rec[s - s0];
+            SF_CUDA(cudaMemcpyAsync(r.pos, d.pos, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+            SF_CUDA(cudaMemcpyAsync(r.vel, d.vel, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+            SF_CUDA(cudaMemcpyAsync(r.cs, d.cell_start, (size_t)d.ncells_pad * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+            sf::DeviceState dr = d;
+            dr.pr = r.pr;
+            dr.rho = r.rho;
+            dr.nbr = r.nbr;
+            dr.nbr_count = r.cnt;
+            dr.sums = r.sums;
+            if (dr.tune.list_mode == SF_LIST_NONE) dr.tune.list_mode = SF_LIST_TILE;
+            sf::launch_density(dr, ctx->c, ctx->stream);
+            sf::launch_force_integrate(dr, ctx->c, ctx->stream);
+            sf::enqueue_sort_tail(d, ctx->stream);
+        }
+        SF_TRY(check_launch("segment recompute"));
+        for (int64_t s = (int64_t)s1 - 1; s >= (int64_t)s0; --s) {
+            const sf::StepRec& r = t->rec[s - s0];
+            sf::AdjointStep st;
+            st.n = n;
+            st.pos = r.pos;
+            st.vel = r.vel;
+            st.pr = r.pr;
+            st.rho = r.rho;
+            st.nbr = r.nbr;
+            st.cnt = r.cnt;
+            st.cs = r.cs;
+            st.sums = r.sums;
+            sf::launch_adjoint_step(st, ctx->c, w, ctx->stream);
+        }
+        SF_TRY(check_launch("adjoint steps"));
+    }
+    SF_TRY(download_by_id(ctx, dloss_dx0, w.Xb));
+    SF_TRY(download_by_id(ctx, dloss_dv0, w.Vb));
+    double sc[2];
+    SF_TRY(copy_out(ctx, sc, w.scalars, sizeof(sc)));
+    const double kPi = 3.14159265358979323846;
+    const double h = ctx->params.kernel_radius, r = ctx->params.particle_radius;
+    const double mass = (double)ctx->params.rest_density * (2.0 * r) * (2.0 * r) * (2.0 * r);
+    const double h6 = h * h * h * h * h * h;
+    if (dloss_dviscosity) *dloss_dviscosity = (float)(sc[0] * (mass * 45.0 / (kPi * h6)));
+    if (dloss_dstiffness) *dloss_dstiffness = (float)sc[1];
+    SF_TRY(restore_sorted(ctx, t->snap));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
     return SF_OK;
 }
 

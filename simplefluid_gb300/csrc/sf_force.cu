@@ -20,7 +20,8 @@ __global__ void __launch_bounds__(kBlockSize)
             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
             uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
             uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-            uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out) {
+            uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
+            float4* __restrict__ sums) {
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     if (i >= n) return;
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
@@ -57,6 +58,10 @@ __global__ void __launch_bounds__(kBlockSize)
             if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)
                 pair_terms(c, xi, vi, pri.x, xj, __ldg(pr + j), ldg4(vel + j), a);
         });
+    }
+    if (sums) {
+        sums[2 * (size_t)i] = make_float4(a.apx, a.apy, a.apz, 0.f);
+        sums[2 * (size_t)i + 1] = make_float4(a.avx, a.avy, a.avz, 0.f);
     }
     const float ax = fmaf(fmaf(c.cp, a.apx, c.cv * a.avx), pri.y, c.g[0]);
     const float ay = fmaf(fmaf(c.cp, a.apy, c.cv * a.avy), pri.y, c.g[1]);
@@ -98,11 +103,11 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
                 k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>
                     <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.nbr,
                                                                      d.nbr_count, d.n, c, d.table, d.scene_off,
-                                                                     d.nscenes, po, vo, co, ks, ac);
+                                                                     d.nscenes, po, vo, co, ks, ac, d.sums);
         } else {
             k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
                 d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ks,
-                ac);
+                ac, d.sums);
         }
     });
 }

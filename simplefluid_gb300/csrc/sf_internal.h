@@ -69,6 +69,7 @@ struct DeviceState {
     float4* accel = nullptr;    // optional acceleration output (inspection)
     uint32_t* nbr = nullptr;       // neighbour lists, tile-major (kNbCap * kNbTile per tile)
     uint32_t* nbr_count = nullptr; // neighbours of each particle (may exceed kNbCap)
+    float4* sums = nullptr;        // optional: per particle (AP, 0), (AV, 0) of the force pass (adjoint recording)
     // grid
     uint32_t ncells = 0, ncells_pad = 0;
     uint32_t* counts = nullptr;      // ncells_pad, zero between steps
@@ -123,6 +124,41 @@ void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);
 constexpr uint32_t kNumStages = 7;
 extern const char* const kStageNames[kNumStages];
 void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s);
+
+// ---- adjoint (sf_adjoint.cu) -------------------------------------------
+// One recorded forward step, in that step's sorted order.
+struct AdjointStep {
+    uint32_t n = 0;
+    const float4* pos = nullptr;
+    const float4* vel = nullptr;
+    const float2* pr = nullptr;
+    const float* rho = nullptr;
+    const uint32_t* nbr = nullptr;
+    const uint32_t* cnt = nullptr;
+    const uint32_t* cs = nullptr;
+    const float4* sums = nullptr;
+};
+// Adjoint working buffers (N particles).  Xb/Vb are indexed by particle id.
+struct AdjointWork {
+    float4* Xb = nullptr;
+    float4* Vb = nullptr;
+    float4* apb = nullptr;
+    float4* avb = nullptr;
+    float4* xdir = nullptr;
+    float4* vdir = nullptr;
+    float4* xf = nullptr;
+    float4* vf = nullptr;
+    float* rhob = nullptr;
+    double2* partial = nullptr;  // adjoint_partial_count(N)
+    double* scalars = nullptr;   // [sum cv_bar, sum k_bar]
+};
+void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, cudaStream_t s);
+uint32_t adjoint_partial_count(uint32_t n);
+// CIC histogram loss of the sorted state; dL/dx written to Xb by particle id.
+void launch_histogram_loss(const float4* pos, uint32_t n, const SimConst& c, const float box_ext[3], uint32_t res,
+                           const float* target, unsigned long long* hist, float* e2, double* partial, float4* Xb,
+                           cudaStream_t s);
+uint32_t histogram_partial_count(uint32_t res);
 
 // Density of caller-owned device positions using the library's fixed static
 // scratch (sf_noalloc.cu); no device allocation.

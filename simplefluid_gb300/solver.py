@@ -212,6 +212,35 @@ class SPHSolver:
         C.check(self._lib.sf_compute_accel(self._ctx, _vp(acc), n))
         return acc
 
+    # -- differentiation ---------------------------------------------------
+    def forward(self, nsteps: int, ckpt_every: int = 20) -> None:
+        """Advance `nsteps` recording checkpoints for :meth:`adjoint`."""
+        C.check(self._lib.sf_forward(self._ctx, int(nsteps), int(ckpt_every)))
+
+    def lossHistogram(self, target: np.ndarray, with_grad: bool = True):
+        """CIC-histogram loss of the current positions against `target` (res^3)."""
+        t = np.ascontiguousarray(target, np.float32)
+        res = int(round(t.size ** (1.0 / 3.0)))
+        if res ** 3 != t.size:
+            raise ValueError("target must have res^3 entries")
+        loss = ctypes.c_double()
+        g = np.empty((self.getNumParticles(), 3), np.float32) if with_grad else None
+        C.check(self._lib.sf_loss_histogram(self._ctx, _vp(t), res, byref(loss), _vp(g)))
+        return (loss.value, g) if with_grad else loss.value
+
+    def adjoint(self, dloss_dx: np.ndarray, dloss_dv: Optional[np.ndarray] = None):
+        """Gradients of the loss w.r.t. the state at the last :meth:`forward` call
+        and w.r.t. viscosity and stiffness: (dx0, dv0, dmu, dk)."""
+        n = self.getNumParticles()
+        gx = np.ascontiguousarray(dloss_dx, np.float32).reshape(n, 3)
+        gv = None if dloss_dv is None else np.ascontiguousarray(dloss_dv, np.float32).reshape(n, 3)
+        dx0 = np.empty((n, 3), np.float32)
+        dv0 = np.empty((n, 3), np.float32)
+        dmu = c_float()
+        dk = c_float()
+        C.check(self._lib.sf_adjoint(self._ctx, _vp(gx), _vp(gv), _vp(dx0), _vp(dv0), byref(dmu), byref(dk)))
+        return dx0, dv0, dmu.value, dk.value
+
     def neighbourStats(self):
         n = self.getNumParticles()
         cnt = np.empty(n, np.uint32)
