@@ -217,6 +217,52 @@ def measure_batched(args) -> dict:
                       "wall clock over the same number of steps per scene"}
 
 
+def measure_adjoint(args) -> dict:
+    """Differentiable dambreak: 65,536 particles, 200 steps, checkpoints every 20;
+    loss = squared distance of the 32^3 CIC histogram to a seeded target.  Reports
+    the plain forward (graph replays, CUDA events), the forward with checkpoints,
+    the loss and the adjoint (wall clock, synchronised), and adjoint / forward."""
+    from simplefluid_gb300 import SPHParameters, SPHSolver, scene_positions
+    prm = SPHParameters(particleRadius=0.005, kernelRadius=0.02, scene=19, pressureStiffness=50.0, viscosity=0.01,
+                        restDensity=1000.0, timeStep=1e-4, boundaryRestitution=0.1)
+    pos = scene_positions(prm, 19)
+    rng = np.random.default_rng(20171)
+    vel = rng.normal(scale=0.05, size=pos.shape).astype(np.float32)
+    target = rng.uniform(size=32 ** 3)
+    target = (target / target.sum()).astype(np.float32)
+    steps, ckpt = 200, 20
+    from simplefluid_gb300 import _capi as C
+    lib = C.load()
+    with SPHSolver(prm) as s:
+        s.setParticles(pos, vel)
+        s.makeReady()
+        s.step(3)
+        s.setParticles(pos, vel)
+        ms = ctypes.c_float()
+        C.check(lib.sf_step_timed(s.handle, steps, 0, ctypes.byref(ms), None))
+        fwd_ms = ms.value
+        best = None
+        for _ in range(3):
+            s.setParticles(pos, vel)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.forward(steps, ckpt)
+            s.synchronize()
+            t1 = time.perf_counter()
+            L, dldx = s.lossHistogram(target)
+            t2 = time.perf_counter()
+            _, dv0, dmu, dk = s.adjoint(dldx)
+            t3 = time.perf_counter()
+            cur = ((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3)
+            best = cur if best is None or cur[2] < best[2] else best
+    return {"particles": int(pos.shape[0]), "steps": steps, "ckpt_every": ckpt, "forward_ms": fwd_ms,
+            "forward_with_checkpoints_ms": best[0], "loss_ms": best[1], "adjoint_ms": best[2],
+            "ratio_adjoint_over_forward": best[2] / fwd_ms, "loss": float(L),
+            "dloss_dviscosity": float(dmu), "dloss_dstiffness": float(dk),
+            "timing": "forward: CUDA events over graph-replayed steps; others: wall clock, best of 3, "
+                      "adjoint includes the checkpointed forward recompute"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
@@ -356,6 +402,7 @@ def run_ours(args, workload):
 
     solver.close()
     batched = measure_batched(args) if (rank == 0 and not args.no_batched) else None
+    adjoint = measure_adjoint(args) if (rank == 0 and not args.no_adjoint) else None
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -384,6 +431,7 @@ def run_ours(args, workload):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "batched": batched,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -400,6 +448,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=100)
     args = ap.parse_args()
     if args.warmup < 3:

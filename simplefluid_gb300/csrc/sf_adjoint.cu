@@ -200,13 +200,28 @@ __global__ void __launch_bounds__(kAdjBlock)
 
 // P4: poly6 density terms onto positions; the step's input adjoints are
 // written back by particle id.
+// Also reduces the step's scalar adjoints (cv_bar in avb.w, k_bar in xf.w) per
+// block, in thread order, into partial[blockIdx.x].
 template <int kReach>
 __global__ void __launch_bounds__(kAdjBlock)
     k_adj_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
                   const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, float m6cd, const float* __restrict__ rhob,
                   const float4* __restrict__ xdir, const float4* __restrict__ vdir, const float4* __restrict__ xf,
-                  const float4* __restrict__ vf, float4* __restrict__ Xb, float4* __restrict__ Vb) {
+                  const float4* __restrict__ vf, const float4* __restrict__ avb, float4* __restrict__ Xb,
+                  float4* __restrict__ Vb, double2* __restrict__ partial) {
+    __shared__ double s0[kAdjBlock], s1[kAdjBlock];
     const uint32_t k = blockIdx.x * kAdjBlock + threadIdx.x;
+    s0[threadIdx.x] = k < n ? (double)avb[k].w : 0.0;
+    s1[threadIdx.x] = k < n ? (double)xf[k].w : 0.0;
+    __syncthreads();
+    for (int o = kAdjBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s0[threadIdx.x] += s0[threadIdx.x + o];
+            s1[threadIdx.x] += s1[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(s0[0], s1[0]);
     if (k >= n) return;
     const float4 xk = pos[k];
     const float rbk = rhob[k];
@@ -226,38 +241,51 @@ __global__ void __launch_bounds__(kAdjBlock)
     Vb[id] = make_float4(vd.x + vfk.x, vd.y + vfk.y, vd.z + vfk.z, 0.f);
 }
 
-// Deterministic reduction of avb[i].w (cv_bar) and xf[i].w (k_bar): per-block
-// partials in double, in thread order; then one block adds them in block order.
-constexpr int kRedBlock = 256;
+// Adds the block partials of `nsteps` steps to acc[0..1]: per step, thread t
+// sums blocks t, t + 256, ... in order, a fixed shared-memory tree combines
+// the threads, and the step sums are added last step first (the order the
+// adjoint visits them).  Deterministic.
+constexpr int kAccThreads = 256;
 
-__global__ void __launch_bounds__(kRedBlock)
-    k_reduce_scalars(const float4* __restrict__ avb, const float4* __restrict__ xf, uint32_t n,
-                     double2* __restrict__ partial) {
-    __shared__ double s0[kRedBlock], s1[kRedBlock];
-    const uint32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    s0[threadIdx.x] = i < n ? (double)avb[i].w : 0.0;
-    s1[threadIdx.x] = i < n ? (double)xf[i].w : 0.0;
-    __syncthreads();
-    for (int o = kRedBlock / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            s0[threadIdx.x] += s0[threadIdx.x + o];
-            s1[threadIdx.x] += s1[threadIdx.x + o];
+__global__ void __launch_bounds__(kAccThreads)
+    k_accumulate_scalars(const double2* __restrict__ partial, uint32_t nsteps, uint32_t nblocks,
+                         double* __restrict__ acc) {
+    __shared__ double s0[kAccThreads], s1[kAccThreads];
+    double a = 0.0, b = 0.0;
+    if (threadIdx.x == 0) {
+        a = acc[0];
+        b = acc[1];
+    }
+    for (int64_t st = (int64_t)nsteps - 1; st >= 0; --st) {
+        double x = 0.0, y = 0.0;
+        for (uint32_t t = threadIdx.x; t < nblocks; t += kAccThreads) {
+            const double2 v = partial[(size_t)st * nblocks + t];
+            x += v.x;
+            y += v.y;
+        }
+        s0[threadIdx.x] = x;
+        s1[threadIdx.x] = y;
+        __syncthreads();
+        for (int o = kAccThreads / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) {
+                s0[threadIdx.x] += s0[threadIdx.x + o];
+                s1[threadIdx.x] += s1[threadIdx.x + o];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            a += s0[0];
+            b += s1[0];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(s0[0], s1[0]);
+    if (threadIdx.x == 0) {
+        acc[0] = a;
+        acc[1] = b;
+    }
 }
 
-__global__ void k_accumulate_scalars(const double2* __restrict__ partial, uint32_t nblocks, double* __restrict__ acc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (uint32_t t = 0; t < nblocks; ++t) {
-        a += partial[t].x;
-        b += partial[t].y;
-    }
-    acc[0] += a;
-    acc[1] += b;
-}
+constexpr int kRedBlock = 256;
 
 // ------------------------------------------------------------------ loss
 // CIC (cloud-in-cell) histogram on res^3 cell-centred bins over the box,
@@ -352,7 +380,8 @@ __global__ void k_hist_grad(const float4* __restrict__ pos, uint32_t n, SimConst
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
-void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, cudaStream_t s) {
+void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
+                         cudaStream_t s) {
     const uint32_t n = st.n;
     if (!n) return;
     const unsigned g = grid_for(n, kAdjBlock);
@@ -364,14 +393,15 @@ void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& 
         k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.apb,
                                                 w.avb, w.rhob, w.xf, w.vf);
         k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.rhob, w.xdir, w.vdir,
-                                                 w.xf, w.vf, w.Xb, w.Vb);
+                                                 w.xf, w.vf, w.avb, w.Xb, w.Vb, partial);
     });
-    const unsigned gr = grid_for(n, kRedBlock);
-    k_reduce_scalars<<<gr, kRedBlock, 0, s>>>(w.avb, w.xf, n, w.partial);
-    k_accumulate_scalars<<<1, 32, 0, s>>>(w.partial, gr, w.scalars);
 }
 
-uint32_t adjoint_partial_count(uint32_t n) { return grid_for(n, kRedBlock); }
+uint32_t adjoint_partial_count(uint32_t n) { return grid_for(n, kAdjBlock); }
+
+void launch_adjoint_accumulate(const double2* partial, uint32_t nsteps, uint32_t n, double* scalars, cudaStream_t s) {
+    k_accumulate_scalars<<<1, kAccThreads, 0, s>>>(partial, nsteps, adjoint_partial_count(n), scalars);
+}
 
 void launch_histogram_loss(const float4* pos, uint32_t n, const SimConst& c, const float box_ext[3], uint32_t res,
                            const float* target, unsigned long long* hist, float* e2, double* partial, float4* Xb,

@@ -36,6 +36,12 @@ struct Trajectory {
     std::vector<float4*> ck;  // per checkpoint: pos then vel (2n float4)
     std::vector<StepRec> rec; // ckpt steps of one segment
     float4* snap = nullptr;   // 2n float4: the forward's final state
+    float4* stage = nullptr;  // 2n float4: the checkpoint a segment graph starts from
+    double2* seg_partial = nullptr;  // ckpt x adjoint_partial_count(n) scalar partials
+    // captured segment graphs (recompute + reverse sweep), by segment length
+    cudaGraphExec_t seg_graph[2] = {nullptr, nullptr};
+    uint32_t seg_len[2] = {0, 0};
+    uint64_t graph_gen = 0;
     AdjointWork w;
     uint32_t hist_res = 0;
     unsigned long long* hist = nullptr;
@@ -46,6 +52,7 @@ struct Trajectory {
 }  // namespace sf
 
 struct sf_ctx {
+    uint64_t gen = 1;  // bumped whenever captured graphs become stale
     sf_params params{};
     sf::SimConst c{};
     sf::DeviceState d{};
@@ -165,14 +172,25 @@ void free_rec(sf::StepRec& r) {
     r = sf::StepRec{};
 }
 
+void drop_segment_graphs(sf::Trajectory* t) {
+    for (int g = 0; g < 2; ++g) {
+        if (t->seg_graph[g]) cudaGraphExecDestroy(t->seg_graph[g]);
+        t->seg_graph[g] = nullptr;
+        t->seg_len[g] = 0;
+    }
+}
+
 void free_trajectory(sf_ctx* ctx) {
     sf::Trajectory* t = ctx->traj;
     if (!t) return;
+    drop_segment_graphs(t);
+    if (t->stage) cudaFree(t->stage);
+    if (t->seg_partial) cudaFree(t->seg_partial);
     for (float4* p : t->ck)
         if (p) cudaFree(p);
     for (auto& r : t->rec) free_rec(r);
     void* b[] = {t->snap, t->w.Xb, t->w.Vb, t->w.apb, t->w.avb, t->w.xdir, t->w.vdir, t->w.xf, t->w.vf,
-                 t->w.rhob, t->w.partial, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
+                 t->w.rhob, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
     for (void* p : b)
         if (p) cudaFree(p);
     delete t;
@@ -182,6 +200,7 @@ void free_trajectory(sf_ctx* ctx) {
 void drop_graph(sf_ctx* ctx) {
     if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
     ctx->step_graph = nullptr;
+    ++ctx->gen;
 }
 
 sf_status alloc_grid(sf_ctx* ctx) {
@@ -1145,7 +1164,6 @@ sf_status ensure_work(sf_ctx* ctx) {
     SF_CUDA(cudaMalloc(&w.xf, n * sizeof(float4)));
     SF_CUDA(cudaMalloc(&w.vf, n * sizeof(float4)));
     SF_CUDA(cudaMalloc(&w.rhob, n * sizeof(float)));
-    SF_CUDA(cudaMalloc(&w.partial, sf::adjoint_partial_count((uint32_t)n) * sizeof(double2)));
     SF_CUDA(cudaMalloc(&w.scalars, 2 * sizeof(double)));
     SF_CUDA(cudaMalloc(&t->snap, 2 * n * sizeof(float4)));
     return SF_OK;
@@ -1155,8 +1173,15 @@ sf_status ensure_records(sf_ctx* ctx, uint32_t ckpt) {
     sf::Trajectory* t = ctx->traj;
     const size_t n = ctx->d.cap;
     const size_t tiles = (n + sf::kNbTile - 1) / sf::kNbTile;
-    if (t->rec.size() == ckpt && t->ncells_pad == ctx->d.ncells_pad) return SF_OK;
+    if (t->rec.size() == ckpt && t->ncells_pad == ctx->d.ncells_pad && t->stage) return SF_OK;
+    drop_segment_graphs(t);
     for (auto& r : t->rec) free_rec(r);
+    if (t->stage) cudaFree(t->stage);
+    if (t->seg_partial) cudaFree(t->seg_partial);
+    t->stage = nullptr;
+    t->seg_partial = nullptr;
+    SF_CUDA(cudaMalloc(&t->stage, 2 * n * sizeof(float4)));
+    SF_CUDA(cudaMalloc(&t->seg_partial, (size_t)ckpt * sf::adjoint_partial_count((uint32_t)n) * sizeof(double2)));
     t->rec.assign(ckpt, sf::StepRec{});
     t->ncells_pad = ctx->d.ncells_pad;
     for (auto& r : t->rec) {
@@ -1203,6 +1228,90 @@ sf_status download_by_id(sf_ctx* ctx, float* dst_xyz, const float4* src) {
         dst_xyz[3 * (size_t)i + 1] = h[i].y;
         dst_xyz[3 * (size_t)i + 2] = h[i].z;
     }
+    return SF_OK;
+}
+
+// Capture one segment of `len` steps: rebuild the cell table of the
+// checkpoint in t->stage, re-run the steps forward recording each step's
+// inputs in its slot (the sort of step s writes the state of step s+1 straight
+// into slot s+1), then the reverse sweep and the scalar accumulation.
+sf_status build_segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
+    sf::Trajectory* t = ctx->traj;
+    sf::DeviceState& d = ctx->d;
+    const uint32_t n = d.n;
+    cudaStream_t st = ctx->stream;
+    cudaGraph_t g = nullptr;
+    SF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    sf::DeviceState r0 = d;
+    r0.pos2 = t->stage;
+    r0.vel2 = t->stage + n;
+    r0.pos = t->rec[0].pos;
+    r0.vel = t->rec[0].vel;
+    r0.cell_start = t->rec[0].cs;
+    sf::launch_hash_count(r0, r0.pos2, n, ctx->c, r0.counts, r0.key_slot, st);
+    sf::enqueue_sort_tail(r0, st);
+    for (uint32_t s = 0; s < len; ++s) {
+        const sf::StepRec& r = t->rec[s];
+        sf::DeviceState ds = d;
+        ds.pos = r.pos;
+        ds.vel = r.vel;
+        ds.cell_start = r.cs;
+        ds.pr = r.pr;
+        ds.rho = r.rho;
+        ds.nbr = r.nbr;
+        ds.nbr_count = r.cnt;
+        ds.sums = r.sums;
+        if (ds.tune.list_mode == SF_LIST_NONE) ds.tune.list_mode = SF_LIST_TILE;
+        sf::launch_density(ds, ctx->c, st);
+        sf::launch_force_integrate(ds, ctx->c, st);
+        sf::DeviceState dn = d;
+        if (s + 1 < len) {
+            dn.pos = t->rec[s + 1].pos;
+            dn.vel = t->rec[s + 1].vel;
+            dn.cell_start = t->rec[s + 1].cs;
+        }
+        sf::enqueue_sort_tail(dn, st);
+    }
+    const uint32_t nb = sf::adjoint_partial_count(n);
+    for (int64_t s = (int64_t)len - 1; s >= 0; --s) {
+        const sf::StepRec& r = t->rec[s];
+        sf::AdjointStep as;
+        as.n = n;
+        as.pos = r.pos;
+        as.vel = r.vel;
+        as.pr = r.pr;
+        as.rho = r.rho;
+        as.nbr = r.nbr;
+        as.cnt = r.cnt;
+        as.cs = r.cs;
+        as.sums = r.sums;
+        sf::launch_adjoint_step(as, ctx->c, t->w, t->seg_partial + (size_t)s * nb, st);
+    }
+    sf::launch_adjoint_accumulate(t->seg_partial, len, n, t->w.scalars, st);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(adjoint segment)");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate(adjoint segment)");
+    }
+    return SF_OK;
+}
+
+sf_status segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
+    sf::Trajectory* t = ctx->traj;
+    for (int k = 0; k < 2; ++k)
+        if (t->seg_graph[k] && t->seg_len[k] == len) {
+            *out = t->seg_graph[k];
+            return SF_OK;
+        }
+    int slot = t->seg_graph[0] ? 1 : 0;
+    if (t->seg_graph[slot]) cudaGraphExecDestroy(t->seg_graph[slot]);
+    t->seg_graph[slot] = nullptr;
+    SF_TRY(build_segment_graph(ctx, len, &t->seg_graph[slot]));
+    t->seg_len[slot] = len;
+    *out = t->seg_graph[slot];
     return SF_OK;
 }
 
@@ -1284,6 +1393,10 @@ SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dlo
     SF_TRY(set_device(ctx));
     SF_TRY(ensure_work(ctx));
     SF_TRY(ensure_records(ctx, t->ckpt));
+    if (t->graph_gen != ctx->gen) {
+        drop_segment_graphs(t);
+        t->graph_gen = ctx->gen;
+    }
     sf::DeviceState& d = ctx->d;
     const uint32_t n = d.n;
     sf::AdjointWork& w = t->w;
@@ -1295,41 +1408,12 @@ SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dlo
     SF_CUDA(cudaMemsetAsync(w.scalars, 0, 2 * sizeof(double), ctx->stream));
     const uint32_t nck = (uint32_t)t->ck.size();
     for (int64_t seg = (int64_t)nck - 1; seg >= 0; --seg) {
-        const uint32_t s0 = (uint32_t)seg * t->ckpt, s1 = std::min(t->nsteps, s0 + t->ckpt);
-        SF_TRY(restore_sorted(ctx, t->ck[seg]));
-        for (uint32_t s = s0; s < s1; ++s) {
-            sf::StepRec& r = t->rec[s - s0];
-            SF_CUDA(cudaMemcpyAsync(r.pos, d.pos, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
-            SF_CUDA(cudaMemcpyAsync(r.vel, d.vel, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
-            SF_CUDA(cudaMemcpyAsync(r.cs, d.cell_start, (size_t)d.ncells_pad * sizeof(uint32_t),
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-            sf::DeviceState dr = d;
-            dr.pr = r.pr;
-            dr.rho = r.rho;
-            dr.nbr = r.nbr;
-            dr.nbr_count = r.cnt;
-            dr.sums = r.sums;
-            if (dr.tune.list_mode == SF_LIST_NONE) dr.tune.list_mode = SF_LIST_TILE;
-            sf::launch_density(dr, ctx->c, ctx->stream);
-            sf::launch_force_integrate(dr, ctx->c, ctx->stream);
-            sf::enqueue_sort_tail(d, ctx->stream);
-        }
-        SF_TRY(check_launch("segment recompute"));
-        for (int64_t s = (int64_t)s1 - 1; s >= (int64_t)s0; --s) {
-            const sf::StepRec& r = t->rec[s - s0];
-            sf::AdjointStep st;
-            st.n = n;
-            st.pos = r.pos;
-            st.vel = r.vel;
-            st.pr = r.pr;
-            st.rho = r.rho;
-            st.nbr = r.nbr;
-            st.cnt = r.cnt;
-            st.cs = r.cs;
-            st.sums = r.sums;
-            sf::launch_adjoint_step(st, ctx->c, w, ctx->stream);
-        }
-        SF_TRY(check_launch("adjoint steps"));
+        const uint32_t s0 = (uint32_t)seg * t->ckpt, len = std::min(t->nsteps, s0 + t->ckpt) - s0;
+        cudaGraphExec_t g = nullptr;
+        SF_TRY(segment_graph(ctx, len, &g));
+        SF_CUDA(cudaMemcpyAsync(t->stage, t->ck[seg], 2 * (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+        SF_CUDA(cudaGraphLaunch(g, ctx->stream));
     }
     SF_TRY(download_by_id(ctx, dloss_dx0, w.Xb));
     SF_TRY(download_by_id(ctx, dloss_dv0, w.Vb));

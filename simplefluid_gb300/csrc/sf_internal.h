@@ -149,11 +149,15 @@ struct AdjointWork {
     float4* xf = nullptr;
     float4* vf = nullptr;
     float* rhob = nullptr;
-    double2* partial = nullptr;  // adjoint_partial_count(N)
     double* scalars = nullptr;   // [sum cv_bar, sum k_bar]
 };
-void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, cudaStream_t s);
+// One step's adjoint; its scalar block partials go to `partial`
+// (adjoint_partial_count(N) entries).
+void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
+                         cudaStream_t s);
 uint32_t adjoint_partial_count(uint32_t n);
+// scalars += the partials of `nsteps` consecutive steps (last step first).
+void launch_adjoint_accumulate(const double2* partial, uint32_t nsteps, uint32_t n, double* scalars, cudaStream_t s);
 // CIC histogram loss of the sorted state; dL/dx written to Xb by particle id.
 void launch_histogram_loss(const float4* pos, uint32_t n, const SimConst& c, const float box_ext[3], uint32_t res,
                            const float* target, unsigned long long* hist, float* e2, double* partial, float4* Xb,
