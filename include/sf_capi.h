@@ -208,6 +208,52 @@ SF_API const char* sf_stage_name(uint32_t stage);
 SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_bytes, float* stage_ms,
                                   uint32_t nstages);
 
+/* ---- headless particle rendering ------------------------------------------------
+ * The arithmetic of the reference's point-sprite sphere impostors
+ * (Shaders/particle.vs.glsl: eye-space position, gl_PointSize = radius *
+ * scale / distance; Shaders/particle.fs.glsl: disc test on gl_PointCoord,
+ * impostor normal, fragment position, Blinn-Phong over up to 8 point lights)
+ * evaluated by CUDA kernels into a device image, without a graphics API.
+ * Visibility: per pixel the fragment with the smallest window depth of its
+ * particle's centre wins (ties: lower particle index), as a depth test on
+ * point sprites without depth correction does.  Image rows run top to bottom. */
+#define SF_COLOR_UNIFORM 0 /* material diffuse                                 */
+#define SF_COLOR_RANDOM 1  /* per-particle colour, uniform in [0,1]^3 from seed */
+#define SF_COLOR_RAMP 2    /* by particle index along PARTICLE_COLOR_RAMP        */
+typedef struct sf_render_params {
+    int32_t width, height;
+    float eye[3], focus[3], up[3]; /* camera: DEFAULT_CAMERA_POSITION/FOCUS, +y up */
+    float fovy_deg, znear, zfar;   /* perspective projection (fovy 55 deg)          */
+    float point_radius;            /* u_PointRadius; 0 = the particle radius         */
+    int32_t num_lights;            /* 1..8                                           */
+    float light_position[8][4];    /* used as given, like the shader does            */
+    float light_ambient[8][4], light_diffuse[8][4], light_specular[8][4];
+    float mat_ambient[4], mat_diffuse[4], mat_specular[4];
+    float mat_shininess;
+    int32_t color_mode;            /* SF_COLOR_*                                     */
+    uint64_t color_seed;
+    float background[4];
+    int32_t reserved[4];
+} sf_render_params;
+/* The reference viewer's settings: 1200 x 1000, camera (-3, 0.8, 0) looking at
+ * (0, -0.2, 0), fovy 55, one light at (-10, 10, 10), CUSTOM_PARTICLE_MATERIAL. */
+SF_API sf_status sf_render_params_default(sf_render_params* rp);
+/* Render the current particles.  rgba_out: width*height*4 floats, depth_out:
+ * width*height floats (1 where empty), owner_out: width*height u32 particle
+ * indices in the caller's order (0xffffffff where empty); any may be NULL. */
+SF_API sf_status sf_render(sf_ctx* ctx, const sf_render_params* rp, float* rgba_out, float* depth_out,
+                           uint32_t* owner_out);
+
+/* ---- state files -------------------------------------------------------------
+ * Not in the reference (it only exports screenshots, Source/MainWindow.cpp:108-113).
+ * A state file holds the parameters, the caller's simulated time and the
+ * particles in the solver's cell-sorted order with their indices; loading it
+ * (parameters included) and stepping reproduces the saved run bit for bit.
+ * Layout: "SFSTATE1", u32 version (1), u32 n, f64 sim_time, sf_params,
+ * n x 3 f32 positions, n x 3 f32 velocities, n u32 caller indices. */
+SF_API sf_status sf_save_state(sf_ctx* ctx, const char* path, double sim_time);
+SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_out);
+
 /* ---- differentiation -------------------------------------------------------
  * Not in the reference.  A hand-written adjoint of the sub-step (density, EOS,
  * forces, integration and box), with each step's neighbour structure held

@@ -67,6 +67,7 @@ def lib() -> ctypes.CDLL:
                                                          c_void_p, c_int]
             getattr(l, f"sfo_loss_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
                                                       c_void_p]
+        l.sfo_render.argtypes = [P, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
         l.sfo_max_threads.argtypes = []
         _lib = l
     return _lib
@@ -231,6 +232,18 @@ def loss(p: sf_params, pos, target, dtype=np.float64):
     _chk(getattr(lib(), f"sfo_loss_{sfx}")(ctypes.byref(p), pos.shape[0], _ptr(pos), _ptr(tgt), res, _ptr(out),
                                            _ptr(g), None), "loss")
     return float(out[0]), g
+
+
+def render(p: sf_params, rp, pos):
+    """CPU restatement of the particle renderer: (rgba HxWx4, depth HxW, owner HxW)."""
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    h, w = rp.height, rp.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    owner = np.zeros((h, w), np.uint32)
+    _chk(lib().sfo_render(ctypes.byref(p), ctypes.byref(rp), pos.shape[0], _ptr(pos), _ptr(rgba), _ptr(depth),
+                          _ptr(owner)), "render")
+    return rgba, depth, owner
 
 
 def max_threads() -> int:

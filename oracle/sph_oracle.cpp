@@ -646,6 +646,123 @@ int grad_impl(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0
     return SF_OK;
 }
 
+
+// ------------------------------------------------------------- rendering --
+// Restatement of the reference's point-sprite shaders (Shaders/particle.vs.glsl:24-35,
+// Shaders/particle.fs.glsl:46-83) as two passes: nearest centre depth per
+// pixel (ties to the lower particle index), then Blinn-Phong shading of the
+// winner.  Matrices follow glm::lookAt / glm::perspective.
+struct RCo {
+    float V[16], P[16], scale, radius;
+    int W, H;
+};
+
+RCo render_const(const sf_render_params* rp, float particle_radius) {
+    RCo rc;
+    double e[3], f[3], u[3], s3[3], uu[3];
+    for (int a = 0; a < 3; ++a) {
+        e[a] = rp->eye[a];
+        f[a] = (double)rp->focus[a] - rp->eye[a];
+        u[a] = rp->up[a];
+    }
+    auto norm = [](double* v) {
+        const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int a = 0; a < 3; ++a) v[a] /= l;
+    };
+    norm(f);
+    s3[0] = f[1] * u[2] - f[2] * u[1];
+    s3[1] = f[2] * u[0] - f[0] * u[2];
+    s3[2] = f[0] * u[1] - f[1] * u[0];
+    norm(s3);
+    uu[0] = s3[1] * f[2] - s3[2] * f[1];
+    uu[1] = s3[2] * f[0] - s3[0] * f[2];
+    uu[2] = s3[0] * f[1] - s3[1] * f[0];
+    double V[16] = {0}, P[16] = {0};
+    for (int a = 0; a < 3; ++a) {
+        V[4 * a] = s3[a];
+        V[4 * a + 1] = uu[a];
+        V[4 * a + 2] = -f[a];
+    }
+    V[12] = -(s3[0] * e[0] + s3[1] * e[1] + s3[2] * e[2]);
+    V[13] = -(uu[0] * e[0] + uu[1] * e[1] + uu[2] * e[2]);
+    V[14] = f[0] * e[0] + f[1] * e[1] + f[2] * e[2];
+    V[15] = 1.0;
+    const double pi = 3.14159265358979323846;
+    const double th = std::tan((double)rp->fovy_deg * 0.5 * pi / 180.0);
+    const double aspect = (double)rp->width / (double)rp->height;
+    P[0] = 1.0 / (aspect * th);
+    P[5] = 1.0 / th;
+    P[10] = -((double)rp->zfar + rp->znear) / ((double)rp->zfar - rp->znear);
+    P[11] = -1.0;
+    P[14] = -(2.0 * rp->zfar * (double)rp->znear) / ((double)rp->zfar - rp->znear);
+    for (int k = 0; k < 16; ++k) {
+        rc.V[k] = (float)V[k];
+        rc.P[k] = (float)P[k];
+    }
+    rc.scale = (float)rp->height / std::tan((float)((double)rp->fovy_deg * 0.5 * pi / 180.0));
+    rc.radius = rp->point_radius > 0.f ? rp->point_radius : particle_radius;
+    rc.W = rp->width;
+    rc.H = rp->height;
+    return rc;
+}
+
+struct SplatO {
+    float e[3], x0, y0, size, depth;
+};
+
+bool splat_o(const RCo& rc, const float* p, SplatO& s) {
+    for (int r = 0; r < 3; ++r) s.e[r] = ((rc.V[r] * p[0] + rc.V[4 + r] * p[1]) + rc.V[8 + r] * p[2]) + rc.V[12 + r];
+    const float dist = std::sqrt((s.e[0] * s.e[0] + s.e[1] * s.e[1]) + s.e[2] * s.e[2]);
+    s.size = rc.radius * (rc.scale / dist);
+    float c[4];
+    for (int r = 0; r < 4; ++r) c[r] = ((rc.P[r] * s.e[0] + rc.P[4 + r] * s.e[1]) + rc.P[8 + r] * s.e[2]) + rc.P[12 + r];
+    if (!(c[3] > 0.f)) return false;
+    if (c[0] < -c[3] || c[0] > c[3] || c[1] < -c[3] || c[1] > c[3] || c[2] < -c[3] || c[2] > c[3]) return false;
+    const float nx = c[0] / c[3], ny = c[1] / c[3], nz = c[2] / c[3];
+    const float wx = (nx * 0.5f + 0.5f) * (float)rc.W;
+    const float wy = (ny * 0.5f + 0.5f) * (float)rc.H;
+    s.depth = nz * 0.5f + 0.5f;
+    s.x0 = wx - s.size * 0.5f;
+    s.y0 = ((float)rc.H - wy) - s.size * 0.5f;
+    return true;
+}
+
+float disc_o(const SplatO& s, int px, int row, float& nx, float& ny) {
+    const float u = (((float)px + 0.5f) - s.x0) / s.size;
+    const float v = (((float)row + 0.5f) - s.y0) / s.size;
+    nx = u * 2.0f + -1.0f;
+    ny = v * -2.0f + 1.0f;
+    return nx * nx + ny * ny;
+}
+
+void normalize_o(float* v) {
+    const float len = std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+    for (int a = 0; a < 3; ++a) v[a] = v[a] / len;
+}
+
+void color_o(const sf_render_params* rp, uint32_t id, uint32_t n, float* col) {
+    if (rp->color_mode == SF_COLOR_RANDOM) {
+        uint64_t z = rp->color_seed ^ ((uint64_t)id * 0x9E3779B97F4A7C15ull);
+        for (int a = 0; a < 3; ++a) {
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t q = z;
+            q = (q ^ (q >> 30)) * 0xBF58476D1CE4E5B9ull;
+            q = (q ^ (q >> 27)) * 0x94D049BB133111EBull;
+            q ^= q >> 31;
+            col[a] = (float)(q >> 40) * (1.0f / 16777216.0f);
+        }
+    } else {
+        static const float ramp[7][3] = {{1.0f, 0.0f, 0.0f}, {1.0f, 0.5f, 0.0f}, {1.0f, 1.0f, 0.0f}, {1.0f, 0.0f, 1.0f},
+                                         {0.0f, 1.0f, 0.0f}, {0.0f, 1.0f, 1.0f}, {0.0f, 0.0f, 1.0f}};
+        const float step = (float)(6.0 / (double)(n > 1 ? n - 1 : 1));
+        const float t = (float)id * step;
+        int k = (int)std::floor(t);
+        k = k < 0 ? 0 : (k > 5 ? 5 : k);
+        const float f = t - (float)k;
+        for (int a = 0; a < 3; ++a) col[a] = std::fma(f, ramp[k + 1][a] - ramp[k][a], ramp[k][a]);
+    }
+}
+
 // ---------------------------------------------------------------- scenes --
 // Restatement of Source/SceneManager.cpp.  Vec3 arithmetic is per component
 // in float, as glm does it.
@@ -932,6 +1049,81 @@ SFO_GRAD(f64, double)
     }
 SFO_ADJ(f32, float)
 SFO_ADJ(f64, double)
+
+// Render n particles given in the caller's order (index = particle id).
+int sfo_render(const sf_params* p, const sf_render_params* rp, uint32_t n, const float* pos3, float* rgba,
+               float* depth, uint32_t* owner) {
+    if (!p || !rp || !pos3 || rp->width <= 0 || rp->height <= 0) return SF_ERR_INVALID_ARGUMENT;
+    const RCo rc = render_const(rp, p->particle_radius);
+    const size_t np = (size_t)rc.W * rc.H;
+    std::vector<uint64_t> keys(np, ~0ull);
+    for (uint32_t i = 0; i < n; ++i) {
+        SplatO s;
+        if (!splat_o(rc, pos3 + 3 * (size_t)i, s) || !(s.size > 0.f)) continue;
+        const int x_lo = std::max((int)std::ceil(s.x0 - 0.5f), 0);
+        const int x_hi = std::min((int)std::ceil(s.x0 + s.size - 0.5f) - 1, rc.W - 1);
+        const int y_lo = std::max((int)std::ceil(s.y0 - 0.5f), 0);
+        const int y_hi = std::min((int)std::ceil(s.y0 + s.size - 0.5f) - 1, rc.H - 1);
+        uint32_t db;
+        std::memcpy(&db, &s.depth, 4);
+        const uint64_t key = ((uint64_t)db << 32) | i;
+        for (int row = y_lo; row <= y_hi; ++row)
+            for (int px = x_lo; px <= x_hi; ++px) {
+                float nx, ny;
+                if (disc_o(s, px, row, nx, ny) > 1.0f) continue;
+                uint64_t& k = keys[(size_t)row * rc.W + px];
+                if (key < k) k = key;
+            }
+    }
+    for (size_t pix = 0; pix < np; ++pix) {
+        const uint64_t key = keys[pix];
+        float out[4] = {rp->background[0], rp->background[1], rp->background[2], rp->background[3]};
+        float dep = 1.0f;
+        uint32_t own = 0xffffffffu;
+        if (key != ~0ull) {
+            const uint32_t id = (uint32_t)(key & 0xffffffffull);
+            SplatO s;
+            splat_o(rc, pos3 + 3 * (size_t)id, s);
+            const int px = (int)(pix % (size_t)rc.W), row = (int)(pix / (size_t)rc.W);
+            float nrm[3];
+            const float mag = disc_o(s, px, row, nrm[0], nrm[1]);
+            nrm[2] = std::sqrt(1.0f - mag);
+            float view[3] = {s.e[0], s.e[1], s.e[2]};
+            normalize_o(view);
+            const float frag[3] = {s.e[0] + nrm[0] * rc.radius, s.e[1] + nrm[1] * rc.radius, s.e[2] + nrm[2] * rc.radius};
+            float surf[3] = {rp->mat_diffuse[0], rp->mat_diffuse[1], rp->mat_diffuse[2]};
+            if (rp->color_mode != SF_COLOR_UNIFORM) color_o(rp, id, n, surf);
+            float shade[3] = {0, 0, 0};
+            for (int l = 0; l < rp->num_lights; ++l) {
+                float ld[3] = {rp->light_position[l][0] - frag[0], rp->light_position[l][1] - frag[1],
+                               rp->light_position[l][2] - frag[2]};
+                normalize_o(ld);
+                float hd[3] = {ld[0] - view[0], ld[1] - view[1], ld[2] - view[2]};
+                normalize_o(hd);
+                const float diff = std::max((nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2], 0.f);
+                const float spec = std::pow(std::max((hd[0] * nrm[0] + hd[1] * nrm[1]) + hd[2] * nrm[2], 0.f),
+                                            rp->mat_shininess);
+                for (int a = 0; a < 3; ++a) {
+                    const float amb = rp->light_ambient[l][a] * rp->mat_ambient[a];
+                    const float dif = (rp->light_diffuse[l][a] * diff) * surf[a];
+                    const float spc = (rp->light_specular[l][a] * spec) * rp->mat_specular[a];
+                    shade[a] += (amb + dif) + spc;
+                }
+            }
+            out[0] = shade[0];
+            out[1] = shade[1];
+            out[2] = shade[2];
+            out[3] = 1.0f;
+            dep = s.depth;
+            own = id;
+        }
+        if (rgba)
+            for (int a = 0; a < 4; ++a) rgba[4 * pix + a] = out[a];
+        if (depth) depth[pix] = dep;
+        if (owner) owner[pix] = own;
+    }
+    return SF_OK;
+}
 
 int sfo_max_threads(void) {
 #ifdef _OPENMP

@@ -9,6 +9,9 @@ from .solver import (  # noqa: F401
     FRAME_TIME,
     SPHBatch,
     batch_cubes,
+    read_state_file,
+    render_params,
+    save_ppm,
     SceneManager,
     Simulator,
     SPHParameters,
@@ -17,5 +20,5 @@ from .solver import (  # noqa: F401
     substeps_per_frame,
 )
 
-__all__ = ["SPHBatch", "batch_cubes", "SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
+__all__ = ["render_params", "save_ppm", "read_state_file", "SPHBatch", "batch_cubes", "SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
            "substeps_per_frame", "FRAME_TIME", "load"]

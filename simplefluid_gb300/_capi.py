@@ -71,6 +71,31 @@ class sf_tuning(ctypes.Structure):
                 ("prefetch", c_int32), ("reserved", c_int32 * 4)]
 
 
+SF_COLOR_UNIFORM = 0
+SF_COLOR_RANDOM = 1
+SF_COLOR_RAMP = 2
+
+
+class sf_render_params(ctypes.Structure):
+    """Mirror of ``struct sf_render_params`` (include/sf_capi.h)."""
+
+    _fields_ = [
+        ("width", c_int32), ("height", c_int32),
+        ("eye", c_float * 3), ("focus", c_float * 3), ("up", c_float * 3),
+        ("fovy_deg", c_float), ("znear", c_float), ("zfar", c_float),
+        ("point_radius", c_float),
+        ("num_lights", c_int32),
+        ("light_position", (c_float * 4) * 8), ("light_ambient", (c_float * 4) * 8),
+        ("light_diffuse", (c_float * 4) * 8), ("light_specular", (c_float * 4) * 8),
+        ("mat_ambient", c_float * 4), ("mat_diffuse", c_float * 4), ("mat_specular", c_float * 4),
+        ("mat_shininess", c_float),
+        ("color_mode", c_int32),
+        ("color_seed", c_uint64),
+        ("background", c_float * 4),
+        ("reserved", c_int32 * 4),
+    ]
+
+
 class SFError(RuntimeError):
     """Raised when a C-ABI call returns a non-zero sf_status."""
 
@@ -115,6 +140,10 @@ PROTOTYPES = {
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
     "sf_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
+    "sf_render_params_default": (c_int32, [_P(sf_render_params)]),
+    "sf_render": (c_int32, [c_void_p, _P(sf_render_params), c_void_p, c_void_p, c_void_p]),
+    "sf_save_state": (c_int32, [c_void_p, c_char_p, c_double]),
+    "sf_load_state": (c_int32, [c_void_p, c_char_p, _P(c_double)]),
     "sf_forward": (c_int32, [c_void_p, c_uint32, c_uint32]),
     "sf_adjoint": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, _P(c_float), _P(c_float)]),
     "sf_loss_histogram": (c_int32, [c_void_p, c_void_p, c_uint32, _P(c_double), c_void_p]),

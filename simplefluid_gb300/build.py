@@ -30,6 +30,7 @@ SOURCES = [
     ("sf_density.cu", ["-fmad=false"]),
     ("sf_force.cu", ["-fmad=false"]),
     ("sf_adjoint.cu", ["-fmad=false"]),
+    ("sf_render.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),

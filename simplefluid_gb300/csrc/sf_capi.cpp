@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "sf_internal.h"
+#include "sf_render.h"
 
 namespace sf {
 // Recorded trajectory of sf_forward and the adjoint's buffers.
@@ -63,6 +64,14 @@ struct sf_ctx {
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
     size_t h_stage_bytes = 0;
     sf::Trajectory* traj = nullptr;  // differentiable runs (sf_forward / sf_adjoint)
+    // render buffers (sf_render)
+    int render_w = 0, render_h = 0;
+    uint32_t render_n = 0;
+    unsigned long long* render_keys = nullptr;
+    float4* render_rgba = nullptr;
+    float* render_depth = nullptr;
+    uint32_t* render_owner = nullptr;
+    uint32_t* render_slot = nullptr;
 };
 
 namespace {
@@ -197,6 +206,19 @@ void free_trajectory(sf_ctx* ctx) {
     ctx->traj = nullptr;
 }
 
+void free_render(sf_ctx* ctx) {
+    void* b[] = {ctx->render_keys, ctx->render_rgba, ctx->render_depth, ctx->render_owner, ctx->render_slot};
+    for (void* p : b)
+        if (p) cudaFree(p);
+    ctx->render_keys = nullptr;
+    ctx->render_rgba = nullptr;
+    ctx->render_depth = nullptr;
+    ctx->render_owner = nullptr;
+    ctx->render_slot = nullptr;
+    ctx->render_w = ctx->render_h = 0;
+    ctx->render_n = 0;
+}
+
 void drop_graph(sf_ctx* ctx) {
     if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
     ctx->step_graph = nullptr;
@@ -320,6 +342,75 @@ sf_status copy_in(sf_ctx* ctx, void* dst, const void* src, size_t bytes) {
 }  // namespace
 
 namespace sf {
+
+void build_render_const(const sf_render_params& rp, float particle_radius, uint32_t n, RenderConst* rc) {
+    // glm::lookAt (right-handed) and glm::perspective, in double
+    double e[3], f[3], u[3], s3[3], uu[3];
+    for (int a = 0; a < 3; ++a) {
+        e[a] = rp.eye[a];
+        f[a] = (double)rp.focus[a] - rp.eye[a];
+        u[a] = rp.up[a];
+    }
+    auto norm = [](double* v) {
+        const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int a = 0; a < 3; ++a) v[a] /= l;
+    };
+    auto cross = [](const double* a, const double* b, double* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    norm(f);
+    cross(f, u, s3);
+    norm(s3);
+    cross(s3, f, uu);
+    double V[16] = {0};
+    for (int a = 0; a < 3; ++a) {
+        V[4 * a + 0] = s3[a];
+        V[4 * a + 1] = uu[a];
+        V[4 * a + 2] = -f[a];
+    }
+    V[12] = -(s3[0] * e[0] + s3[1] * e[1] + s3[2] * e[2]);
+    V[13] = -(uu[0] * e[0] + uu[1] * e[1] + uu[2] * e[2]);
+    V[14] = f[0] * e[0] + f[1] * e[1] + f[2] * e[2];
+    V[15] = 1.0;
+    const double kPi = 3.14159265358979323846;
+    const double th = std::tan((double)rp.fovy_deg * 0.5 * kPi / 180.0);
+    const double aspect = (double)rp.width / (double)rp.height;
+    const double zn = rp.znear, zf = rp.zfar;
+    double P[16] = {0};
+    P[0] = 1.0 / (aspect * th);
+    P[5] = 1.0 / th;
+    P[10] = -(zf + zn) / (zf - zn);
+    P[11] = -1.0;
+    P[14] = -(2.0 * zf * zn) / (zf - zn);
+    for (int k = 0; k < 16; ++k) {
+        rc->V[k] = (float)V[k];
+        rc->P[k] = (float)P[k];
+    }
+    // u_PointScale = height / tanf(fovy / 2) (Source/FluidRenderWidget.cpp:66)
+    rc->scale = (float)rp.height / std::tan((float)((double)rp.fovy_deg * 0.5 * kPi / 180.0));
+    rc->radius = rp.point_radius > 0.f ? rp.point_radius : particle_radius;
+    rc->width = rp.width;
+    rc->height = rp.height;
+    rc->num_lights = rp.num_lights;
+    std::memcpy(rc->light_position, rp.light_position, sizeof(rc->light_position));
+    std::memcpy(rc->light_ambient, rp.light_ambient, sizeof(rc->light_ambient));
+    std::memcpy(rc->light_diffuse, rp.light_diffuse, sizeof(rc->light_diffuse));
+    std::memcpy(rc->light_specular, rp.light_specular, sizeof(rc->light_specular));
+    std::memcpy(rc->mat_ambient, rp.mat_ambient, sizeof(rc->mat_ambient));
+    std::memcpy(rc->mat_diffuse, rp.mat_diffuse, sizeof(rc->mat_diffuse));
+    std::memcpy(rc->mat_specular, rp.mat_specular, sizeof(rc->mat_specular));
+    rc->mat_shininess = rp.mat_shininess;
+    rc->color_mode = rp.color_mode;
+    rc->color_seed = rp.color_seed;
+    // PARTICLE_COLOR_RAMP (Include/Common.h:33-42)
+    const float ramp[kRampColors][3] = {{1.0f, 0.0f, 0.0f}, {1.0f, 0.5f, 0.0f}, {1.0f, 1.0f, 0.0f}, {1.0f, 0.0f, 1.0f},
+                                        {0.0f, 1.0f, 0.0f}, {0.0f, 1.0f, 1.0f}, {0.0f, 0.0f, 1.0f}};
+    std::memcpy(rc->ramp, ramp, sizeof(ramp));
+    rc->ramp_step = (float)((double)(kRampColors - 1) / (double)(n > 1 ? n - 1 : 1));
+    std::memcpy(rc->background, rp.background, sizeof(rc->background));
+}
 
 int derive_constants(const sf_params& p, SimConst* c, const char** why) {
     const double h = p.kernel_radius, r = p.particle_radius;
@@ -492,6 +583,7 @@ SF_API sf_status sf_destroy(sf_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_trajectory(ctx);
+    free_render(ctx);
     drop_graph(ctx);
     free_particles(ctx->d);
     free_grid(ctx->d);
@@ -859,6 +951,161 @@ SF_API sf_status sf_density_noalloc(const sf_params* p, const float* d_pos_xyz, 
     if (st) return fail(st, why);
     st = sf::noalloc_density(*p, c, d_pos_xyz, n, d_rho, d_pressure, static_cast<cudaStream_t>(stream), &why);
     if (st) return fail(st, why);
+    return SF_OK;
+}
+
+// ---------------------------------------------------------------- rendering
+SF_API sf_status sf_render_params_default(sf_render_params* rp) {
+    if (!rp) return fail(SF_ERR_INVALID_ARGUMENT, "null render parameters");
+    std::memset(rp, 0, sizeof(*rp));
+    rp->width = 1200;  // FluidRenderWidget default size (Source/FluidRenderWidget.cpp:23)
+    rp->height = 1000;
+    const float eye[3] = {-3.0f, 0.8f, 0.0f}, focus[3] = {0.0f, -0.2f, 0.0f}, up[3] = {0.0f, 1.0f, 0.0f};
+    for (int a = 0; a < 3; ++a) {
+        rp->eye[a] = eye[a];  // DEFAULT_CAMERA_POSITION (Include/Common.h:21)
+        rp->focus[a] = focus[a];  // DEFAULT_CAMERA_FOCUS (Include/Common.h:22)
+        rp->up[a] = up[a];
+    }
+    rp->fovy_deg = 55.0f;  // Source/FluidRenderWidget.cpp:66
+    rp->znear = 0.1f;
+    rp->zfar = 1000.0f;
+    rp->num_lights = 1;  // Source/FluidRenderWidget.cpp:91-93
+    const float lp[4] = {-10.0f, 10.0f, 10.0f, 1.0f};
+    for (int a = 0; a < 4; ++a) {
+        rp->light_position[0][a] = lp[a];
+        rp->light_ambient[0][a] = 1.0f;
+        rp->light_diffuse[0][a] = 1.0f;
+        rp->light_specular[0][a] = 1.0f;
+    }
+    // CUSTOM_PARTICLE_MATERIAL (Include/Common.h:24-31)
+    const float ma = 0.2f * 0.2f, md[4] = {1.0f, 0.63f, 0.3f, 1.0f};
+    for (int a = 0; a < 4; ++a) {
+        rp->mat_ambient[a] = ma;
+        rp->mat_diffuse[a] = md[a];
+        rp->mat_specular[a] = 1.0f;
+    }
+    rp->mat_shininess = 250.0f;
+    rp->color_mode = SF_COLOR_UNIFORM;
+    rp->color_seed = 20171;
+    return SF_OK;
+}
+
+SF_API sf_status sf_render(sf_ctx* ctx, const sf_render_params* rp, float* rgba_out, float* depth_out,
+                           uint32_t* owner_out) {
+    SF_TRY(need_sorted(ctx));
+    if (!rp) return fail(SF_ERR_INVALID_ARGUMENT, "null render parameters");
+    if (rp->width <= 0 || rp->height <= 0 || (int64_t)rp->width * rp->height > (1 << 26))
+        return fail(SF_ERR_INVALID_ARGUMENT, "image size out of range");
+    if (rp->num_lights < 0 || rp->num_lights > 8) return fail(SF_ERR_INVALID_ARGUMENT, "num_lights must be 0..8");
+    if (rp->color_mode < SF_COLOR_UNIFORM || rp->color_mode > SF_COLOR_RAMP)
+        return fail(SF_ERR_INVALID_ARGUMENT, "unknown color_mode");
+    if (!(rp->fovy_deg > 0.f && rp->fovy_deg < 180.f) || !(rp->znear > 0.f) || !(rp->zfar > rp->znear))
+        return fail(SF_ERR_INVALID_ARGUMENT, "bad projection");
+    SF_TRY(set_device(ctx));
+    const uint32_t n = ctx->d.n;
+    if (ctx->render_w != rp->width || ctx->render_h != rp->height || ctx->render_n < ctx->d.cap) {
+        free_render(ctx);
+        const size_t np = (size_t)rp->width * rp->height;
+        SF_CUDA(cudaMalloc(&ctx->render_keys, np * sizeof(unsigned long long)));
+        SF_CUDA(cudaMalloc(&ctx->render_rgba, np * sizeof(float4)));
+        SF_CUDA(cudaMalloc(&ctx->render_depth, np * sizeof(float)));
+        SF_CUDA(cudaMalloc(&ctx->render_owner, np * sizeof(uint32_t)));
+        SF_CUDA(cudaMalloc(&ctx->render_slot, (size_t)ctx->d.cap * sizeof(uint32_t)));
+        ctx->render_w = rp->width;
+        ctx->render_h = rp->height;
+        ctx->render_n = ctx->d.cap;
+    }
+    sf::RenderConst rc;
+    sf::build_render_const(*rp, ctx->params.particle_radius, n, &rc);
+    sf::launch_render(ctx->d.pos, n, rc, ctx->render_keys, ctx->render_slot, ctx->render_rgba, ctx->render_depth,
+                      ctx->render_owner, ctx->stream);
+    SF_TRY(check_launch("render"));
+    const size_t np = (size_t)rp->width * rp->height;
+    if (rgba_out) SF_TRY(copy_out(ctx, rgba_out, ctx->render_rgba, np * sizeof(float4)));
+    if (depth_out) SF_TRY(copy_out(ctx, depth_out, ctx->render_depth, np * sizeof(float)));
+    if (owner_out) SF_TRY(copy_out(ctx, owner_out, ctx->render_owner, np * sizeof(uint32_t)));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+// ---------------------------------------------------------------- state files
+// Layout (little endian): "SFSTATE1", u32 version = 1, u32 n, f64 sim_time,
+// sf_params, then n x 3 f32 positions, n x 3 f32 velocities and n u32
+// particle indices, all in the solver's cell-sorted order.  Loading restores
+// that order, so stepping a loaded state reproduces the saved run bit for bit.
+// The n x 3 arrays can be read directly for offline use; particle i of the
+// caller's order is at the row whose index entry is i.
+SF_API sf_status sf_save_state(sf_ctx* ctx, const char* path, double sim_time) {
+    SF_TRY(need_sorted(ctx));
+    if (!path) return fail(SF_ERR_INVALID_ARGUMENT, "null path");
+    SF_TRY(set_device(ctx));
+    const uint32_t n = ctx->d.n;
+    uint32_t* ids_dev = ctx->d.tmp;
+    sf::launch_store_sorted(ctx->d.pos, ctx->d.vel, n, ctx->d.io, ctx->d.io + 3 * (size_t)n, ids_dev, ctx->stream);
+    SF_TRY(check_launch("store sorted"));
+    std::vector<float> pv(6 * (size_t)n);
+    std::vector<uint32_t> ids(n);
+    SF_TRY(copy_out(ctx, pv.data(), ctx->d.io, pv.size() * sizeof(float)));
+    SF_TRY(copy_out(ctx, ids.data(), ids_dev, ids.size() * sizeof(uint32_t)));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(SF_ERR_INVALID_ARGUMENT, std::string("cannot open for writing: ") + path);
+    const char magic[8] = {'S', 'F', 'S', 'T', 'A', 'T', 'E', '1'};
+    const uint32_t version = 1;
+    bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(&version, 4, 1, f) == 1 && std::fwrite(&n, 4, 1, f) == 1 &&
+              std::fwrite(&sim_time, 8, 1, f) == 1 && std::fwrite(&ctx->params, sizeof(sf_params), 1, f) == 1 &&
+              std::fwrite(pv.data(), sizeof(float), pv.size(), f) == pv.size() &&
+              std::fwrite(ids.data(), sizeof(uint32_t), ids.size(), f) == ids.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(SF_ERR_INVALID_ARGUMENT, std::string("write failed: ") + path);
+    return SF_OK;
+}
+
+SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_out) {
+    SF_TRY(need_ctx(ctx));
+    if (!path) return fail(SF_ERR_INVALID_ARGUMENT, "null path");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(SF_ERR_INVALID_ARGUMENT, std::string("cannot open: ") + path);
+    char magic[8];
+    uint32_t version = 0, n = 0;
+    double t = 0.0;
+    sf_params p{};
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "SFSTATE1", 8) == 0 &&
+              std::fread(&version, 4, 1, f) == 1 && version == 1 && std::fread(&n, 4, 1, f) == 1 &&
+              std::fread(&t, 8, 1, f) == 1 && std::fread(&p, sizeof(sf_params), 1, f) == 1;
+    std::vector<float> pv;
+    std::vector<uint32_t> ids;
+    if (ok) {
+        pv.resize(6 * (size_t)n);
+        ids.resize(n);
+        ok = std::fread(pv.data(), sizeof(float), pv.size(), f) == pv.size() &&
+             std::fread(ids.data(), sizeof(uint32_t), ids.size(), f) == ids.size();
+    }
+    std::fclose(f);
+    if (!ok) return fail(SF_ERR_INVALID_ARGUMENT, std::string("not a valid state file: ") + path);
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t id : ids) {
+        if (id >= n || seen[id]) return fail(SF_ERR_INVALID_ARGUMENT, "state file indices are not a permutation");
+        seen[id] = 1;
+    }
+    SF_TRY(sf_set_params(ctx, &p));
+    SF_TRY(set_device(ctx));
+    const bool resized = n != ctx->d.n;
+    SF_TRY(alloc_particles(ctx, n));
+    if (resized) drop_graph(ctx);
+    ctx->d.n = n;
+    ctx->sorted = false;
+    if (n) {
+        sf::DeviceState& d = ctx->d;
+        SF_TRY(copy_in(ctx, d.io, pv.data(), pv.size() * sizeof(float)));
+        SF_TRY(copy_in(ctx, d.tmp, ids.data(), ids.size() * sizeof(uint32_t)));
+        sf::launch_load_sorted(d.io, d.io + 3 * (size_t)n, d.tmp, n, d.pos2, d.vel2, ctx->stream);
+        sf::launch_hash_count(d, d.pos2, n, ctx->c, d.counts, d.key_slot, ctx->stream);
+        sf::enqueue_sort_tail(d, ctx->stream);
+        SF_TRY(check_launch("load state"));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->sorted = true;
+    }
+    if (sim_time_out) *sim_time_out = t;
     return SF_OK;
 }
 

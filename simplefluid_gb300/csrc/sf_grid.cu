@@ -25,6 +25,31 @@ __global__ void k_load_aos(const float* __restrict__ pos3, const float* __restri
         vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Sorted state with explicit particle indices (state files).
+__global__ void k_load_sorted(const float* __restrict__ pos3, const float* __restrict__ vel3,
+                              const uint32_t* __restrict__ ids, uint32_t n, float4* __restrict__ pos,
+                              float4* __restrict__ vel) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pos[i] = make_float4(pos3[3 * (size_t)i], pos3[3 * (size_t)i + 1], pos3[3 * (size_t)i + 2], __uint_as_float(ids[i]));
+    vel[i] = make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.f);
+}
+
+// Sorted state out (state files): AoS pos/vel in solver order plus indices.
+__global__ void k_store_sorted(const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
+                               float* __restrict__ pos3, float* __restrict__ vel3, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i], v = vel[i];
+    pos3[3 * (size_t)i] = p.x;
+    pos3[3 * (size_t)i + 1] = p.y;
+    pos3[3 * (size_t)i + 2] = p.z;
+    vel3[3 * (size_t)i] = v.x;
+    vel3[3 * (size_t)i + 1] = v.y;
+    vel3[3 * (size_t)i + 2] = v.z;
+    ids[i] = __float_as_uint(p.w);
+}
+
 __global__ void k_store_aos(const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
                             float* __restrict__ pos3, float* __restrict__ vel3) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -183,6 +208,16 @@ __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t
 // ---------------------------------------------------------------- launchers
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s) {
     if (n) k_load_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, n, pos, vel);
+}
+
+void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* ids, uint32_t n, float4* pos,
+                        float4* vel, cudaStream_t s) {
+    if (n) k_load_sorted<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, ids, n, pos, vel);
+}
+
+void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, uint32_t* ids,
+                         cudaStream_t s) {
+    if (n) k_store_sorted<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, vel, n, pos3, vel3, ids);
 }
 
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s) {

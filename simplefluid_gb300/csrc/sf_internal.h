@@ -96,6 +96,10 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 
 // ---- kernel launchers (sf_kernels.cu); all enqueue on `s` ---------------
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
+void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* ids, uint32_t n, float4* pos,
+                        float4* vel, cudaStream_t s);
+void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, uint32_t* ids,
+                         cudaStream_t s);
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s);
 void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,
                        uint2* key_slot, cudaStream_t s);

@@ -212,6 +212,30 @@ class SPHSolver:
         C.check(self._lib.sf_compute_accel(self._ctx, _vp(acc), n))
         return acc
 
+    # -- headless rendering ------------------------------------------------
+    def render(self, rp: Optional[C.sf_render_params] = None):
+        """Sphere-impostor image of the particles: (rgba HxWx4, depth HxW, owner HxW)."""
+        rp = rp or render_params()
+        h, w = rp.height, rp.width
+        rgba = np.empty((h, w, 4), np.float32)
+        depth = np.empty((h, w), np.float32)
+        owner = np.empty((h, w), np.uint32)
+        C.check(self._lib.sf_render(self._ctx, byref(rp), _vp(rgba), _vp(depth), _vp(owner)))
+        return rgba, depth, owner
+
+    # -- state files -----------------------------------------------------
+    def saveState(self, path: str, sim_time: float = 0.0) -> None:
+        C.check(self._lib.sf_save_state(self._ctx, str(path).encode(), float(sim_time)))
+
+    def loadState(self, path: str) -> float:
+        """Load parameters and state (solver order kept); returns the saved sim time."""
+        t = ctypes.c_double()
+        C.check(self._lib.sf_load_state(self._ctx, str(path).encode(), byref(t)))
+        pr = C.sf_params()
+        C.check(self._lib.sf_get_params(self._ctx, byref(pr)))
+        self.params = SPHParameters.from_c(pr)
+        return t.value
+
     # -- differentiation ---------------------------------------------------
     def forward(self, nsteps: int, ckpt_every: int = 20) -> None:
         """Advance `nsteps` recording checkpoints for :meth:`adjoint`."""
@@ -402,6 +426,53 @@ class Simulator:
             self.particleChanged()
         if self.numParticleChanged:
             self.numParticleChanged(self.m_SPHSolver.getNumParticles())
+
+
+def render_params(**kw) -> C.sf_render_params:
+    """The reference viewer's render settings, with keyword overrides."""
+    rp = C.sf_render_params()
+    C.check(C.load().sf_render_params_default(byref(rp)))
+    for k, v in kw.items():
+        if k in ("eye", "focus", "up", "background"):
+            for a, x in enumerate(v):
+                getattr(rp, k)[a] = x
+        else:
+            setattr(rp, k, v)
+    return rp
+
+
+def save_ppm(path: str, rgba: np.ndarray) -> None:
+    """Write an RGBA float image (rows top to bottom) as an 8-bit binary PPM."""
+    img = (np.clip(rgba[..., :3], 0.0, 1.0) * 255.0 + 0.5).astype(np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (img.shape[1], img.shape[0]))
+        f.write(img.tobytes())
+
+
+STATE_MAGIC = b"SFSTATE1"
+
+
+def read_state_file(path: str):
+    """Read a state file (no GPU needed): dict with sim_time, params, and
+    positions/velocities in the caller's particle order."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    if raw[:8] != STATE_MAGIC:
+        raise ValueError("not a SimpleFluid state file")
+    version, n = np.frombuffer(raw, np.uint32, 2, 8)
+    if version != 1:
+        raise ValueError(f"unsupported state file version {version}")
+    t = float(np.frombuffer(raw, np.float64, 1, 16)[0])
+    psize = ctypes.sizeof(C.sf_params)
+    params = C.sf_params.from_buffer_copy(raw[24:24 + psize])
+    off = 24 + psize
+    pv = np.frombuffer(raw, np.float32, 6 * int(n), off)
+    ids = np.frombuffer(raw, np.uint32, int(n), off + 24 * int(n))
+    pos = np.empty((int(n), 3), np.float32)
+    vel = np.empty((int(n), 3), np.float32)
+    pos[ids] = pv[:3 * int(n)].reshape(-1, 3)
+    vel[ids] = pv[3 * int(n):].reshape(-1, 3)
+    return {"sim_time": t, "params": params, "positions": pos, "velocities": vel, "solver_order": ids.copy()}
 
 
 def batch_cubes(seed: int, nscenes: int, base: SPHParameters):

@@ -368,3 +368,33 @@ def test_tuning_rejects_bad_values(lib):
     for bad in (C.sf_tuning(7, 128, 128, 2), C.sf_tuning(1, 64, 128, 2), C.sf_tuning(1, 128, 128, 3)):
         assert lib.sf_set_tuning(s.handle, ctypes.byref(bad)) == C.SF_ERR_INVALID_ARGUMENT
     s.close()
+
+
+def test_full_size_sphere_pool(oracle):
+    """Sphere drop into a pool: a jittered pool of depth 0.3 over the unit
+    footprint plus a jittered sphere of radius 0.15 at one particle spacing
+    (r = 0.00227, h = 4r).  At one spacing the geometry holds ~3.35M
+    particles (the pool ~3.19M, the sphere ~0.15M), the count recorded here.
+    Sort, cell table and density are checked against the oracle at full size;
+    after 10 steps the size-independent properties hold."""
+    prm = params_1m(particleRadius=0.00227, kernelRadius=0.00908, scene=C.SF_SCENE_SPHERE_POOL)
+    pos = scene_positions(prm, C.SF_SCENE_SPHERE_POOL)
+    n = pos.shape[0]
+    assert 3_300_000 < n < 3_400_000
+    st = oracle.State(pos)
+    okeys, ocs = st.sort(prm.to_c(), want_cells=True)
+    orho, _, _ = st.density(prm.to_c())
+    with solver_with(prm, pos) as s:
+        _, _, ids, keys = s.sortedState()
+        assert np.array_equal(ids, st.ids) and np.array_equal(keys, okeys)
+        assert np.array_equal(s.cellStart(), ocs)
+        grho, _ = s.computeDensity()
+        assert np.array_equal(grho.view(np.uint32), orho.view(np.uint32))
+        s.step(10)
+        _, _, ids, keys = s.sortedState()
+        gpos, gvel = s.getState()
+    assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+    assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
+    assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
+    lo, hi = np.float32(0.00227), np.float32(1 - 0.00227)
+    assert np.all(gpos >= lo) and np.all(gpos <= hi)
