@@ -92,7 +92,12 @@ typedef struct sf_params {
                                         the (2K+1)^3 cells around a particle's cell
                                         and the summation order follows the grid,
                                         so K is part of the arithmetic.            */
-    int32_t reserved[2];             /* must be zero                                */
+    int32_t adaptive_time_step;      /* 0: every sub-step is time_step.  1: CFL
+                                        sub-step dt = min(time_step,
+                                        0.4 h / max|v|, 0.25 sqrt(h / max|a|)),
+                                        maxima over the previous sub-step (the
+                                        initial state's |v| for the first)      */
+    int32_t reserved[1];             /* must be zero                                */
 } sf_params;
 
 typedef struct sf_ctx sf_ctx;
@@ -138,9 +143,17 @@ SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out);
 /* ---- stepping: makeReady() / advanceFrame() ----------------------------- */
 /* Build the uniform grid, sort the particles and capture the step graph. */
 SF_API sf_status sf_make_ready(sf_ctx* ctx);
-/* One fixed sub-step; *dt_out receives the simulated time advanced.  The
- * work is queued on the context's stream; the call does not wait for it. */
+/* One sub-step; *dt_out receives the simulated time advanced.  With a fixed
+ * time step the work is queued and the call does not wait; with the adaptive
+ * step it waits to read the sub-step's dt (pass NULL to skip the wait). */
 SF_API sf_status sf_advance_frame(sf_ctx* ctx, float* dt_out);
+/* Whole frames on the device: per frame, sub-steps are taken until their dt,
+ * summed in float, reach frame_time (the loop of Source/Simulator.cpp:46-51,
+ * frame_time 0.0333333333) or max_substeps were taken.  Each frame is one CUDA
+ * graph launch whose sub-step loop is a device-side conditional while node.
+ * Waits; reports the simulated time and the sub-steps taken in total. */
+SF_API sf_status sf_advance_frames(sf_ctx* ctx, uint32_t frames, double frame_time, uint32_t max_substeps,
+                                   double* sim_time_out, uint32_t* substeps_out);
 /* `nsteps` sub-steps, queued as replays of one captured step graph. */
 SF_API sf_status sf_step(sf_ctx* ctx, uint32_t nsteps);
 /* Wait for all queued work of the context. */

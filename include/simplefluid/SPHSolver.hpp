@@ -141,6 +141,17 @@ public:
         m_HostStale = true;
     }
 
+    // Whole frames on the device (sub-steps until frame_time, one graph
+    // launch per frame); returns the simulated time advanced.
+    double advanceFrames(uint32_t frames, double frame_time = 0.0333333333, uint32_t max_substeps = 100000,
+                         uint32_t* substeps = nullptr) {
+        upload_if_dirty();
+        double t = 0.0;
+        check(sf_advance_frames(m_Ctx, frames, frame_time, max_substeps, &t, substeps));
+        m_HostStale = true;
+        return t;
+    }
+
     unsigned int getNumParticles() {
         if (m_HostDirty) return (unsigned int)m_Particles.size();
         uint32_t n = 0;
@@ -264,9 +275,14 @@ public:
         m_SPHSolver->makeReady();
         while (m_SimTime < m_SimParams->stopTime && !m_bStop) {
             float frameTime = 0;
-            while (frameTime < 0.0333333333) {
-                frameTime += m_SPHSolver->advanceFrame();
-                if (particleChanged) particleChanged();
+            if (!particleChanged) {
+                // no per-sub-step observer: the whole frame on the device
+                frameTime = (float)m_SPHSolver->advanceFrames(1);
+            } else {
+                while (frameTime < 0.0333333333) {
+                    frameTime += m_SPHSolver->advanceFrame();
+                    particleChanged();
+                }
             }
             m_SimTime += frameTime;
             if (systemTimeChanged) systemTimeChanged(m_SimTime);

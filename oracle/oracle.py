@@ -68,6 +68,8 @@ def lib() -> ctypes.CDLL:
             getattr(l, f"sfo_loss_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
                                                       c_void_p]
         l.sfo_render.argtypes = [P, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.sfo_frames_f32.argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_uint32, ctypes.c_double, c_uint32,
+                                     c_int, POINTER(ctypes.c_double), POINTER(c_uint32), c_void_p, c_uint32]
         l.sfo_max_threads.argtypes = []
         _lib = l
     return _lib
@@ -176,6 +178,17 @@ class State:
     def step(self, p: sf_params, nsteps: int = 1, threads: int = 0):
         _chk(getattr(lib(), f"sfo_step_{self.sfx}")(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel),
                                                     _ptr(self.ids), nsteps, threads), "step")
+
+    def frames(self, p: sf_params, frames: int, frame_time: float = 0.0333333333, max_substeps: int = 100000,
+               threads: int = 0, record_dts: int = 0):
+        """The frame loop (FP32); returns (sim_time, substeps, dts of the first `record_dts` sub-steps)."""
+        t = ctypes.c_double()
+        k = c_uint32()
+        dts = np.zeros(record_dts, np.float32) if record_dts else None
+        _chk(lib().sfo_frames_f32(ctypes.byref(p), self.n, _ptr(self.pos), _ptr(self.vel), _ptr(self.ids), frames,
+                                  frame_time, max_substeps, threads, ctypes.byref(t), ctypes.byref(k), _ptr(dts),
+                                  record_dts), "frames")
+        return t.value, k.value, dts
 
     def original_order(self):
         """Positions and velocities in the caller's original particle order."""

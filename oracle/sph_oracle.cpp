@@ -55,7 +55,7 @@ struct Derived {
     Real h, h2, mass, cd, cp, cv, k, rho0, inv_rho0, dt, e, r;
     Real g[3], lo[3], hi[3], bmin[3], inv_cell[3];
     int n[3];
-    int eos, attractive, reach;
+    int eos, attractive, reach, adaptive;
     uint64_t ncells;
 };
 
@@ -81,6 +81,7 @@ int derive(const sf_params* p, Derived<Real>* d) {
     d->r = (Real)r;
     d->eos = p->eos;
     d->attractive = p->use_attractive_pressure;
+    d->adaptive = p->adaptive_time_step;
     const int K = p->cells_per_h ? p->cells_per_h : 2;
     if (K < 1 || K > 3) return SF_ERR_INVALID_ARGUMENT;
     d->reach = K;
@@ -282,12 +283,12 @@ void accel_pass(const Derived<Real>& d, uint32_t n, const Real* pos, const Real*
 }
 
 template <typename Real>
-void integrate_pass(const Derived<Real>& d, uint32_t n, Real* pos, Real* vel, const Real* acc) {
+void integrate_pass(const Derived<Real>& d, uint32_t n, Real* pos, Real* vel, const Real* acc, Real dt) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
         for (int a = 0; a < 3; ++a) {
-            Real v = std::fma(d.dt, acc[3 * i + a], vel[3 * i + a]);
-            Real x = std::fma(d.dt, v, pos[3 * i + a]);
+            Real v = std::fma(dt, acc[3 * i + a], vel[3 * i + a]);
+            Real x = std::fma(dt, v, pos[3 * i + a]);
             if (x < d.lo[a]) {
                 x = d.lo[a];
                 if (v < (Real)0) v = -d.e * v;
@@ -302,6 +303,49 @@ void integrate_pass(const Derived<Real>& d, uint32_t n, Real* pos, Real* vel, co
     }
 }
 
+// One sub-step after another, with the sub-step rule of the context: fixed
+// dt, or the adaptive dt = min(dt_max, 0.4 h / max|v|, 0.25 sqrt(h / max|a|))
+// from the maxima of the previous sub-step (|v| after integration; for the
+// first sub-step max|v| of the initial state and no acceleration term).
+template <typename Real>
+struct SubStepper {
+    const Derived<Real>& d;
+    uint32_t n;
+    Real v2max = 0, a2max = 0, last_dt = 0;
+    std::vector<uint32_t> keys, cs;
+    std::vector<Real> prs, inv, acc;
+    SubStepper(const Derived<Real>& dd, uint32_t nn, const Real* vel) : d(dd), n(nn), prs(nn), inv(nn), acc(3 * (size_t)nn) {
+        for (uint32_t i = 0; i < n; ++i) v2max = std::max(v2max, sq3(vel + 3 * (size_t)i));
+    }
+    static Real sq3(const Real* v) { return std::fma(v[2], v[2], std::fma(v[1], v[1], v[0] * v[0])); }
+    Real choose_dt() const {
+        Real dt = d.dt;
+        if (d.adaptive) {
+            const Real cfl_v = (Real)0.4f, cfl_a = (Real)0.25f;
+            if (v2max > (Real)0) dt = std::min(dt, (cfl_v * d.h) / std::sqrt(v2max));
+            if (a2max > (Real)0) dt = std::min(dt, cfl_a * std::sqrt(d.h / std::sqrt(a2max)));
+        }
+        return dt;
+    }
+    void step(Real* pos, Real* vel, uint32_t* ids) {
+        const Real dt = choose_dt();
+        sort_and_grid(d, n, pos, vel, ids, keys, cs);
+        density_pass(d, n, pos, cs, (Real*)nullptr, prs.data(), inv.data());
+        accel_pass(d, n, pos, vel, prs.data(), inv.data(), cs, acc.data());
+        integrate_pass(d, n, pos, vel, acc.data(), dt);
+        if (d.adaptive) {
+            Real vm = 0, am = 0;
+            for (uint32_t i = 0; i < n; ++i) {
+                vm = std::max(vm, sq3(vel + 3 * (size_t)i));
+                am = std::max(am, sq3(&acc[3 * (size_t)i]));
+            }
+            v2max = vm;
+            a2max = am;
+        }
+        last_dt = dt;
+    }
+};
+
 template <typename Real>
 int step_impl(const sf_params* p, uint32_t n, Real* pos, Real* vel, uint32_t* ids, uint32_t nsteps,
               int threads) {
@@ -311,14 +355,8 @@ int step_impl(const sf_params* p, uint32_t n, Real* pos, Real* vel, uint32_t* id
     if (n == 0) return SF_OK;
     if (!pos || !vel || !ids) return SF_ERR_INVALID_ARGUMENT;
     set_threads(threads);
-    std::vector<uint32_t> keys, cs;
-    std::vector<Real> prs(n), inv_rho(n), acc(3 * (size_t)n);
-    for (uint32_t s = 0; s < nsteps; ++s) {
-        sort_and_grid(d, n, pos, vel, ids, keys, cs);
-        density_pass(d, n, pos, cs, (Real*)nullptr, prs.data(), inv_rho.data());
-        accel_pass(d, n, pos, vel, prs.data(), inv_rho.data(), cs, acc.data());
-        integrate_pass(d, n, pos, vel, acc.data());
-    }
+    SubStepper<Real> stepper(d, n, vel);
+    for (uint32_t s = 0; s < nsteps; ++s) stepper.step(pos, vel, ids);
     return SF_OK;
 }
 
@@ -593,7 +631,7 @@ int grad_impl(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0
         sort_and_grid(d, n, pos.data(), vel.data(), ids.data(), keys, cs);
         density_pass(d, n, pos.data(), cs, (Real*)nullptr, prs.data(), inv.data());
         accel_pass(d, n, pos.data(), vel.data(), prs.data(), inv.data(), cs, acc.data());
-        integrate_pass(d, n, pos.data(), vel.data(), acc.data());
+        integrate_pass(d, n, pos.data(), vel.data(), acc.data(), d.dt);
     }
     // loss at the final state (array order = the last step's sorted order)
     std::vector<Real> Xb(n3, (Real)0), Vb(n3, (Real)0);
@@ -630,7 +668,7 @@ int grad_impl(const sf_params* p, uint32_t n, const Real* pos0, const Real* vel0
             density_pass(d, n, ps.data(), R.cs, R.rho.data(), R.prs.data(), R.inv.data());
             accel_pass(d, n, ps.data(), vs.data(), R.prs.data(), R.inv.data(), R.cs, acc.data(), R.ap.data(),
                        R.av.data());
-            integrate_pass(d, n, ps.data(), vs.data(), acc.data());
+            integrate_pass(d, n, ps.data(), vs.data(), acc.data(), d.dt);
         }
         for (int64_t s = (int64_t)s1 - 1; s >= (int64_t)s0; --s) adjoint_step(d, n, recs[s - s0], Xb.data(), Vb.data(), &mub, &kb);
     }
@@ -981,7 +1019,7 @@ int sfo_scene(const sf_params* p, int scene, uint64_t seed, float* pos3, uint32_
         Derived<Real> d;                                                                                    \
         int st = derive(p, &d);                                                                             \
         if (st) return st;                                                                                  \
-        integrate_pass(d, n, pos, vel, acc);                                                                \
+        integrate_pass(d, n, pos, vel, acc, d.dt);                                                          \
         return SF_OK;                                                                                       \
     }                                                                                                       \
     int sfo_neighbour_stats_##SUFFIX(const sf_params* p, uint32_t n, const Real* pos, const uint32_t* ids,   \
@@ -1122,6 +1160,36 @@ int sfo_render(const sf_params* p, const sf_render_params* rp, uint32_t n, const
         if (depth) depth[pix] = dep;
         if (owner) owner[pix] = own;
     }
+    return SF_OK;
+}
+
+// The frame loop of Source/Simulator.cpp:46-51: per frame, sub-steps until
+// their dt summed in float reach frame_time (or max_substeps were taken).
+int sfo_frames_f32(const sf_params* p, uint32_t n, float* pos, float* vel, uint32_t* ids, uint32_t frames,
+                   double frame_time, uint32_t max_substeps, int threads, double* sim_time, uint32_t* substeps,
+                   float* dts, uint32_t dts_cap) {
+    Derived<float> d;
+    int st = derive(p, &d);
+    if (st) return st;
+    if (!pos || !vel || !ids || n == 0 || max_substeps == 0) return SF_ERR_INVALID_ARGUMENT;
+    set_threads(threads);
+    SubStepper<float> stp(d, n, vel);
+    double t = 0.0;
+    uint32_t total = 0;
+    for (uint32_t f = 0; f < frames; ++f) {
+        float acc = 0.0f;
+        uint32_t it = 0;
+        do {
+            stp.step(pos, vel, ids);
+            if (dts && total < dts_cap) dts[total] = stp.last_dt;
+            acc = acc + stp.last_dt;
+            t += (double)stp.last_dt;
+            ++it;
+            ++total;
+        } while ((double)acc < frame_time && it < max_substeps);
+    }
+    if (sim_time) *sim_time = t;
+    if (substeps) *substeps = total;
     return SF_OK;
 }
 

@@ -55,7 +55,8 @@ class sf_params(ctypes.Structure):
         ("box_max", c_float * 3),
         ("eos", c_int32),
         ("cells_per_h", c_int32),
-        ("reserved", c_int32 * 2),
+        ("adaptive_time_step", c_int32),
+        ("reserved", c_int32 * 1),
     ]
 
 
@@ -124,6 +125,7 @@ PROTOTYPES = {
     "sf_make_ready": (c_int32, [c_void_p]),
     "sf_advance_frame": (c_int32, [c_void_p, _P(c_float)]),
     "sf_step": (c_int32, [c_void_p, c_uint32]),
+    "sf_advance_frames": (c_int32, [c_void_p, c_uint32, c_double, c_uint32, _P(c_double), _P(c_uint32)]),
     "sf_synchronize": (c_int32, [c_void_p]),
     "sf_get_stream": (c_int32, [c_void_p, _P(c_void_p)]),
     "sf_host_alloc": (c_int32, [c_size_t, _P(c_void_p)]),

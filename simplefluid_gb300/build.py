@@ -31,6 +31,7 @@ SOURCES = [
     ("sf_force.cu", ["-fmad=false"]),
     ("sf_adjoint.cu", ["-fmad=false"]),
     ("sf_render.cu", ["-fmad=false"]),
+    ("sf_frame.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),

@@ -64,6 +64,11 @@ struct sf_ctx {
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
     size_t h_stage_bytes = 0;
     sf::Trajectory* traj = nullptr;  // differentiable runs (sf_forward / sf_adjoint)
+    sf::FrameState* frame = nullptr;  // device sub-step / frame state
+    cudaGraphExec_t frame_graph = nullptr;
+    uint64_t frame_graph_gen = 0;
+    double frame_graph_time = 0.0;
+    uint32_t frame_graph_max = 0;
     // render buffers (sf_render)
     int render_w = 0, render_h = 0;
     uint32_t render_n = 0;
@@ -122,7 +127,9 @@ sf_status validate(const sf_params& p) {
     if (p.num_threads < 0) return fail(SF_ERR_INVALID_ARGUMENT, "num_threads must be >= 0");
     if (p.cells_per_h < 0 || p.cells_per_h > 3)
         return fail(SF_ERR_INVALID_ARGUMENT, "cells_per_h must be 1, 2 or 3 (0 = 2)");
-    if (p.reserved[0] || p.reserved[1]) return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    if (p.adaptive_time_step != 0 && p.adaptive_time_step != 1)
+        return fail(SF_ERR_INVALID_ARGUMENT, "adaptive_time_step must be 0 or 1");
+    if (p.reserved[0]) return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
     for (int a = 0; a < 3; ++a) {
         if (!finite(p.gravity[a]) || !finite(p.box_min[a]) || !finite(p.box_max[a]))
             return fail(SF_ERR_INVALID_ARGUMENT, "gravity and box must be finite");
@@ -279,16 +286,30 @@ sf_status sort_uploaded(sf_ctx* ctx) {
     sf::launch_load_aos(d.io, d.io + 3 * (size_t)d.n, d.n, d.pos2, d.vel2, ctx->stream);
     sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
     sf::enqueue_sort_tail(d, ctx->stream);
+    if (ctx->frame) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
     SF_TRY(check_launch("initial sort"));
     ctx->sorted = true;
     return SF_OK;
+}
+
+// The step as launched: with the adaptive sub-step, dt is chosen on the
+// device first and the force pass reads it and raises the maxima.
+void enqueue_full_step(sf_ctx* ctx) {
+    if (ctx->c.adaptive) {
+        sf::DeviceState dr = ctx->d;
+        dr.frame = ctx->frame;
+        sf::launch_choose_dt(ctx->frame, ctx->c, ctx->stream);
+        sf::enqueue_step(dr, ctx->c, ctx->stream);
+    } else {
+        sf::enqueue_step(ctx->d, ctx->c, ctx->stream);
+    }
 }
 
 sf_status capture_step(sf_ctx* ctx) {
     drop_graph(ctx);
     cudaGraph_t g = nullptr;
     SF_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    sf::enqueue_step(ctx->d, ctx->c, ctx->stream);
+    enqueue_full_step(ctx);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(step)");
     e = cudaGraphInstantiate(&ctx->step_graph, g, 0);
@@ -431,6 +452,9 @@ int derive_constants(const sf_params& p, SimConst* c, const char** why) {
     c->eos = p.eos;
     c->attractive = p.use_attractive_pressure ? 1 : 0;
     c->cell_base = 0;
+    c->adaptive = p.adaptive_time_step ? 1 : 0;
+    c->cfl_v = 0.4f;
+    c->cfl_a = 0.25f;
     const int K = p.cells_per_h ? p.cells_per_h : 2;
     c->reach = K;
     double coord_max = 0.0;
@@ -570,6 +594,11 @@ SF_API sf_status sf_create(const sf_params* p, sf_ctx** out) {
         return cuda_fail(e, "stream creation");
     }
     st = alloc_grid(ctx);
+    if (!st) {
+        e = cudaMalloc(&ctx->frame, sizeof(sf::FrameState));
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->frame, 0, sizeof(sf::FrameState), ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "frame state");
+    }
     if (st) {
         sf_destroy(ctx);
         return st;
@@ -584,6 +613,8 @@ SF_API sf_status sf_destroy(sf_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_trajectory(ctx);
     free_render(ctx);
+    if (ctx->frame_graph) cudaGraphExecDestroy(ctx->frame_graph);
+    if (ctx->frame) cudaFree(ctx->frame);
     drop_graph(ctx);
     free_particles(ctx->d);
     free_grid(ctx->d);
@@ -606,9 +637,11 @@ SF_API sf_status sf_set_params(sf_ctx* ctx, const sf_params* p) {
     const bool grid_changed = std::memcmp(c.n, ctx->c.n, sizeof(c.n)) != 0 ||
                               std::memcmp(c.bmin, ctx->c.bmin, sizeof(c.bmin)) != 0 ||
                               std::memcmp(c.inv_cell, ctx->c.inv_cell, sizeof(c.inv_cell)) != 0;
+    const bool became_adaptive = c.adaptive && !ctx->c.adaptive;
     ctx->params = *p;
     ctx->c = c;
     drop_graph(ctx);
+    if (became_adaptive && ctx->sorted && ctx->d.n) sf::launch_init_maxima(ctx->d.vel, ctx->d.n, ctx->frame, ctx->stream);
     if (grid_changed) {
         SF_TRY(alloc_grid(ctx));
         if (ctx->sorted && ctx->d.n) {
@@ -688,7 +721,77 @@ SF_API sf_status sf_make_ready(sf_ctx* ctx) {
 
 SF_API sf_status sf_advance_frame(sf_ctx* ctx, float* dt_out) {
     SF_TRY(sf_step(ctx, 1));
-    if (dt_out) *dt_out = ctx->params.time_step;
+    if (!dt_out) return SF_OK;
+    if (!ctx->c.adaptive) {
+        *dt_out = ctx->params.time_step;
+        return SF_OK;
+    }
+    SF_CUDA(cudaMemcpyAsync(dt_out, &ctx->frame->dt, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+}
+
+// One frame as a graph: reset the frame clock, then a conditional while node
+// whose body is one sub-step followed by the frame check.
+static sf_status build_frame_graph(sf_ctx* ctx, double frame_time, uint32_t max_substeps, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    SF_CUDA(cudaGraphCreate(&g, 0));
+    struct GraphGuard {
+        cudaGraph_t g;
+        ~GraphGuard() {
+            if (g) cudaGraphDestroy(g);
+        }
+    } guard{g};
+    cudaGraphConditionalHandle h;
+    SF_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    SF_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    sf::launch_frame_begin(ctx->frame, ctx->stream);
+    cudaGraph_t captured = nullptr;
+    SF_CUDA(cudaStreamEndCapture(ctx->stream, &captured));
+    size_t nn = 0;
+    SF_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    SF_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    SF_CUDA(cudaGraphAddNode(&cn, g, nodes.data(), nullptr, nn, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    SF_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    sf::DeviceState dr = ctx->d;
+    dr.frame = ctx->frame;
+    sf::launch_choose_dt(ctx->frame, ctx->c, ctx->stream);
+    sf::enqueue_step(dr, ctx->c, ctx->stream);
+    sf::launch_frame_check(ctx->frame, frame_time, max_substeps, h, ctx->stream);
+    SF_CUDA(cudaStreamEndCapture(ctx->stream, &body));
+    SF_CUDA(cudaGraphInstantiate(out, g, 0));
+    return SF_OK;
+}
+
+SF_API sf_status sf_advance_frames(sf_ctx* ctx, uint32_t frames, double frame_time, uint32_t max_substeps,
+                                   double* sim_time_out, uint32_t* substeps_out) {
+    SF_TRY(sf_make_ready(ctx));
+    if (!(frame_time > 0.0) || max_substeps == 0) return fail(SF_ERR_INVALID_ARGUMENT, "need frame_time > 0, max_substeps > 0");
+    if (!ctx->frame_graph || ctx->frame_graph_gen != ctx->gen || ctx->frame_graph_time != frame_time ||
+        ctx->frame_graph_max != max_substeps) {
+        if (ctx->frame_graph) cudaGraphExecDestroy(ctx->frame_graph);
+        ctx->frame_graph = nullptr;
+        SF_TRY(build_frame_graph(ctx, frame_time, max_substeps, &ctx->frame_graph));
+        ctx->frame_graph_gen = ctx->gen;
+        ctx->frame_graph_time = frame_time;
+        ctx->frame_graph_max = max_substeps;
+    }
+    SF_CUDA(cudaMemsetAsync(&ctx->frame->substeps, 0, sizeof(uint32_t), ctx->stream));
+    SF_CUDA(cudaMemsetAsync(&ctx->frame->sim_time, 0, sizeof(double), ctx->stream));
+    for (uint32_t f = 0; f < frames; ++f) SF_CUDA(cudaGraphLaunch(ctx->frame_graph, ctx->stream));
+    sf::FrameState fs;
+    SF_CUDA(cudaMemcpyAsync(&fs, ctx->frame, sizeof(fs), cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (sim_time_out) *sim_time_out = fs.sim_time;
+    if (substeps_out) *substeps_out = fs.substeps;
     return SF_OK;
 }
 
@@ -1101,6 +1204,7 @@ SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_o
         sf::launch_load_sorted(d.io, d.io + 3 * (size_t)n, d.tmp, n, d.pos2, d.vel2, ctx->stream);
         sf::launch_hash_count(d, d.pos2, n, ctx->c, d.counts, d.key_slot, ctx->stream);
         sf::enqueue_sort_tail(d, ctx->stream);
+        sf::launch_init_maxima(d.vel, n, ctx->frame, ctx->stream);
         SF_TRY(check_launch("load state"));
         SF_CUDA(cudaStreamSynchronize(ctx->stream));
         ctx->sorted = true;
@@ -1201,6 +1305,8 @@ SF_API sf_status sf_batch_create(const sf_params* per_scene, uint32_t nscenes, s
         if (Ks != K) return fail(SF_ERR_INVALID_ARGUMENT, "all scenes of a batch must share cells_per_h");
     }
     if (K > 2) return fail(SF_ERR_INVALID_ARGUMENT, "batches support cells_per_h 1 or 2");
+    for (uint32_t s = 0; s < nscenes; ++s)
+        if (per_scene[s].adaptive_time_step) return fail(SF_ERR_INVALID_ARGUMENT, "batches use a fixed time step");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -1568,6 +1674,7 @@ extern "C" {
 
 SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every) {
     SF_TRY(sf_make_ready(ctx));
+    if (ctx->c.adaptive) return fail(SF_ERR_INVALID_ARGUMENT, "differentiation needs a fixed time step");
     if (ckpt_every == 0) return fail(SF_ERR_INVALID_ARGUMENT, "ckpt_every must be > 0");
     if (!ctx->traj) ctx->traj = new sf::Trajectory();
     sf::Trajectory* t = ctx->traj;

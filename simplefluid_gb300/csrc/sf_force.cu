@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(kBlockSize)
             uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
             uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
-            float4* __restrict__ sums) {
+            float4* __restrict__ sums, FrameState* __restrict__ frame) {
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     if (i >= n) return;
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(kBlockSize)
         acc_out[i] = make_float4(ax, ay, az, 0.f);
         return;
     }
-    float v[3] = {fmaf(c.dt, ax, vi.x), fmaf(c.dt, ay, vi.y), fmaf(c.dt, az, vi.z)};
-    float x[3] = {fmaf(c.dt, v[0], xi.x), fmaf(c.dt, v[1], xi.y), fmaf(c.dt, v[2], xi.z)};
+    const float dt = frame ? frame->dt : c.dt;
+    float v[3] = {fmaf(dt, ax, vi.x), fmaf(dt, ay, vi.y), fmaf(dt, az, vi.z)};
+    float x[3] = {fmaf(dt, v[0], xi.x), fmaf(dt, v[1], xi.y), fmaf(dt, v[2], xi.z)};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         if (x[q] < c.lo[q]) {
@@ -87,6 +88,17 @@ __global__ void __launch_bounds__(kBlockSize)
     vel_out[i] = make_float4(v[0], v[1], v[2], 0.f);
     const uint32_t key = cell_key(c, x[0], x[1], x[2]);
     key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+    if (frame && c.adaptive) {
+        // maxima of |v'|^2 and |a|^2 (non-negative floats order like their bits)
+        const unsigned mask = __activemask();
+        const uint32_t v2 = __float_as_uint(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
+        const uint32_t a2 = __float_as_uint(fmaf(az, az, fmaf(ay, ay, ax * ax)));
+        const uint32_t mv = __reduce_max_sync(mask, v2), ma = __reduce_max_sync(mask, a2);
+        if ((threadIdx.x & 31) == (uint32_t)(__ffs(mask) - 1)) {
+            atomicMax(&frame->v2max_bits, mv);
+            atomicMax(&frame->a2max_bits, ma);
+        }
+    }
 }
 
 template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate>
@@ -103,11 +115,11 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
                 k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>
                     <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.nbr,
                                                                      d.nbr_count, d.n, c, d.table, d.scene_off,
-                                                                     d.nscenes, po, vo, co, ks, ac, d.sums);
+                                                                     d.nscenes, po, vo, co, ks, ac, d.sums, nullptr);
         } else {
             k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
                 d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ks,
-                ac, d.sums);
+                ac, d.sums, kIntegrate ? d.frame : nullptr);
         }
     });
 }

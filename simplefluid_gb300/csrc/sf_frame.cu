@@ -1,0 +1,72 @@
+// sf_frame.cu — sub-step control on the device: the adaptive (CFL) sub-step
+// and the frame loop of Source/Simulator.cpp:46-51 ("while frameTime < 1/30:
+// frameTime += advanceFrame()") as the body of a CUDA-graph conditional while
+// node, so a whole frame is one graph launch with no host round trip.
+//
+// Adaptive sub-step: dt = min(time_step, 0.4 h / max|v|, 0.25 sqrt(h / max|a|))
+// with both maxima taken over the previous sub-step (|v| after integration),
+// which keeps forces and integration in one fused pass.  The CPU oracle
+// restates the same rule.
+#include "sf_device.cuh"
+
+namespace sf {
+namespace {
+
+__global__ void k_choose_dt(FrameState* __restrict__ fs, SimConst c) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    float dt = c.dt;
+    if (c.adaptive) {
+        const float v2 = __uint_as_float(fs->v2max_bits), a2 = __uint_as_float(fs->a2max_bits);
+        if (v2 > 0.f) dt = fminf(dt, (c.cfl_v * c.h) / sqrtf(v2));
+        if (a2 > 0.f) dt = fminf(dt, c.cfl_a * sqrtf(c.h / sqrtf(a2)));
+    }
+    fs->dt = dt;
+    fs->v2max_bits = 0u;
+    fs->a2max_bits = 0u;
+}
+
+__global__ void k_init_maxima(const float4* __restrict__ vel, uint32_t n, FrameState* __restrict__ fs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t v2 = 0u;
+    if (i < n) {
+        const float4 v = vel[i];
+        v2 = __float_as_uint(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
+    }
+    const uint32_t m = __reduce_max_sync(0xffffffffu, v2);
+    if ((threadIdx.x & 31) == 0) atomicMax(&fs->v2max_bits, m);
+}
+
+__global__ void k_frame_begin(FrameState* __restrict__ fs) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    fs->frame_acc = 0.f;
+    fs->iter = 0u;
+}
+
+__global__ void k_frame_check(FrameState* __restrict__ fs, double frame_time, uint32_t max_substeps,
+                              cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float dt = fs->dt;
+    fs->frame_acc = fs->frame_acc + dt;
+    fs->iter += 1u;
+    fs->substeps += 1u;
+    fs->sim_time += (double)dt;
+    cudaGraphSetConditional(h, ((double)fs->frame_acc < frame_time && fs->iter < max_substeps) ? 1u : 0u);
+}
+
+}  // namespace
+
+void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s) { k_choose_dt<<<1, 32, 0, s>>>(fs, c); }
+
+void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s) {
+    cudaMemsetAsync(&fs->v2max_bits, 0, 2 * sizeof(uint32_t), s);
+    if (n) k_init_maxima<<<grid_for(n, kBlock), kBlock, 0, s>>>(vel, n, fs);
+}
+
+void launch_frame_begin(FrameState* fs, cudaStream_t s) { k_frame_begin<<<1, 32, 0, s>>>(fs); }
+
+void launch_frame_check(FrameState* fs, double frame_time, uint32_t max_substeps, cudaGraphConditionalHandle h,
+                        cudaStream_t s) {
+    k_frame_check<<<1, 32, 0, s>>>(fs, frame_time, max_substeps, h);
+}
+
+}  // namespace sf

@@ -33,6 +33,20 @@ struct SimConst {
     float prune_margin;
     float prune_h2;
     uint32_t cell_base;   // first key of this scene's cells (0 outside a batch)
+    // adaptive sub-step: dt = min(dt_max, cfl_v h / max|v|, cfl_a sqrt(h / max|a|))
+    int adaptive;
+    float cfl_v, cfl_a;
+};
+
+// Device-side frame and sub-step state (one per context).
+struct FrameState {
+    float dt;            // the current sub-step
+    uint32_t v2max_bits; // max |v|^2 of the last sub-step (float bits, >= 0)
+    uint32_t a2max_bits; // max |a|^2 of the last sub-step
+    float frame_acc;     // simulated time of the current frame (float, like frameTime)
+    uint32_t iter;       // sub-steps of the current frame
+    uint32_t substeps;   // sub-steps since the last reset
+    double sim_time;     // simulated time since the last reset
 };
 
 // Fill `c` from `p`; returns SF_OK or an error code (with message in `why`).
@@ -70,6 +84,7 @@ struct DeviceState {
     uint32_t* nbr = nullptr;       // neighbour lists, tile-major (kNbCap * kNbTile per tile)
     uint32_t* nbr_count = nullptr; // neighbours of each particle (may exceed kNbCap)
     float4* sums = nullptr;        // optional: per particle (AP, 0), (AV, 0) of the force pass (adjoint recording)
+    FrameState* frame = nullptr;   // adaptive sub-steps read dt here and raise the maxima
     // grid
     uint32_t ncells = 0, ncells_pad = 0;
     uint32_t* counts = nullptr;      // ncells_pad, zero between steps
@@ -128,6 +143,17 @@ void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);
 constexpr uint32_t kNumStages = 7;
 extern const char* const kStageNames[kNumStages];
 void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s);
+
+// ---- sub-step control (sf_frame.cu) ------------------------------------
+// dt of the next sub-step from the maxima (adaptive) or the fixed step; clears the maxima.
+void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s);
+// Maxima of the uploaded state: |v|^2 over the particles, |a|^2 = 0.
+void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s);
+void launch_frame_begin(FrameState* fs, cudaStream_t s);
+// frame_acc += dt, count the sub-step, continue the while node while
+// (double)frame_acc < frame_time and iter < max_substeps.
+void launch_frame_check(FrameState* fs, double frame_time, uint32_t max_substeps, cudaGraphConditionalHandle h,
+                        cudaStream_t s);
 
 // ---- adjoint (sf_adjoint.cu) -------------------------------------------
 // One recorded forward step, in that step's sorted order.

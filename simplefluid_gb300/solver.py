@@ -51,6 +51,7 @@ class SPHParameters:
     boxMax: tuple = (1.0, 1.0, 1.0)
     eos: int = C.SF_EOS_LINEAR
     cellsPerH: int = 2
+    adaptiveTimeStep: bool = False
 
     def to_c(self) -> C.sf_params:
         p = C.sf_params()
@@ -71,6 +72,7 @@ class SPHParameters:
         p.time_step = self.timeStep
         p.eos = int(self.eos)
         p.cells_per_h = int(self.cellsPerH)
+        p.adaptive_time_step = 1 if self.adaptiveTimeStep else 0
         return p
 
     @classmethod
@@ -79,7 +81,8 @@ class SPHParameters:
                    pressureStiffness=p.pressure_stiffness, boundaryRestitution=p.boundary_restitution,
                    viscosity=p.viscosity, stopTime=p.stop_time, bUseAttractivePressure=bool(p.use_attractive_pressure),
                    scene=p.scene, restDensity=p.rest_density, gravity=tuple(p.gravity), timeStep=p.time_step,
-                   boxMin=tuple(p.box_min), boxMax=tuple(p.box_max), eos=p.eos, cellsPerH=p.cells_per_h)
+                   boxMin=tuple(p.box_min), boxMax=tuple(p.box_max), eos=p.eos, cellsPerH=p.cells_per_h,
+                   adaptiveTimeStep=bool(p.adaptive_time_step))
 
     def updateParams(self) -> None:
         """SPHParameters::updateParams() (Source/Controller.cpp:63): validate."""
@@ -174,6 +177,14 @@ class SPHSolver:
 
     def step(self, nsteps: int) -> None:
         C.check(self._lib.sf_step(self._ctx, int(nsteps)))
+
+    def advanceFrames(self, frames: int, frame_time: float = 0.0333333333, max_substeps: int = 100000):
+        """Whole frames on the device; returns (simulated time, sub-steps taken)."""
+        t = ctypes.c_double()
+        k = c_uint32()
+        C.check(self._lib.sf_advance_frames(self._ctx, int(frames), float(frame_time), int(max_substeps), byref(t),
+                                            byref(k)))
+        return t.value, k.value
 
     def synchronize(self) -> None:
         C.check(self._lib.sf_synchronize(self._ctx))
@@ -332,8 +343,9 @@ class Simulator:
     Qt signals become optional callbacks: ``particleChanged`` (per sub-step,
     Source/Simulator.cpp:50), ``systemTimeChanged`` / ``frameFinished`` (per
     frame, :54-55), ``simulationFinished`` (:60), ``numParticleChanged`` (:102).
-    With no ``particleChanged`` callback a frame's sub-steps are queued as one
-    ``sf_step`` call (same arithmetic, no per-sub-step host round trip).
+    With no ``particleChanged`` callback a frame runs on the device as one
+    graph launch (``sf_advance_frames``: same arithmetic, no per-sub-step host
+    round trip).
     """
 
     def __init__(self, params: Optional[SPHParameters] = None, seed: int = 20171):
@@ -380,14 +392,12 @@ class Simulator:
     def doSimulation(self) -> None:
         solver = self.m_SPHSolver
         solver.makeReady()
-        k = substeps_per_frame(self.m_SimParams.timeStep)
-        dt = np.float32(self.m_SimParams.timeStep)
         while float(self.m_SimTime) < self.m_SimParams.stopTime and not self.m_bStop:
             frame_time = np.float32(0.0)
             if self.particleChanged is None:
-                solver.step(k)
-                for _ in range(k):
-                    frame_time = np.float32(frame_time + dt)
+                # the whole frame on the device: one graph launch
+                t, _ = solver.advanceFrames(1, FRAME_TIME)
+                frame_time = np.float32(t)
             else:
                 while float(frame_time) < FRAME_TIME:
                     frame_time = np.float32(frame_time + np.float32(solver.advanceFrame()))

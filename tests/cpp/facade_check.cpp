@@ -5,6 +5,7 @@
 // output file.  Used by tests/test_facade.py.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 
 #include "simplefluid/SPHSolver.hpp"
@@ -39,6 +40,22 @@ int main(int argc, char** argv) {
         out.write(reinterpret_cast<const char*>(pos.data()), n * sizeof(simplefluid::Vec3f));
         out.write(reinterpret_cast<const char*>(vel.data()), n * sizeof(simplefluid::Vec3f));
         std::printf("particles=%u substeps=%d frames=%d simtime=%.6f\n", nparticles, substeps, nframes, sim.simTime());
+        // the same frames with no per-sub-step observer run on the device
+        {
+            simplefluid::Simulator sim2;
+            *sim2.getSimParams() = *params;
+            int frames2 = 0;
+            sim2.frameFinished = [&] { ++frames2; };
+            sim2.setupScene();
+            sim2.startSimulation();
+            sim2.wait();
+            const auto& pos2 = sim2.solver().particles();
+            if (frames2 != nframes || pos2.size() != pos.size() ||
+                std::memcmp(pos2.data(), pos.data(), pos.size() * sizeof(simplefluid::Vec3f)) != 0) {
+                std::fprintf(stderr, "device frame loop differs from the per-sub-step loop\n");
+                return 1;
+            }
+        }
         // the error path: an invalid parameter throws simplefluid::Error
         try {
             params->kernelRadius = -1.f;
