@@ -71,6 +71,7 @@ struct SPHParameters {
     std::array<Real, 3> boxMax{Real(1), Real(1), Real(1)};
     int eos = SF_EOS_LINEAR;
     int cellsPerH = 2;
+    bool adaptiveTimeStep = false;
 
     sf_params toC() const {
         sf_params p{};
@@ -93,6 +94,7 @@ struct SPHParameters {
         p.time_step = (float)timeStep;
         p.eos = eos;
         p.cells_per_h = cellsPerH;
+        p.adaptive_time_step = adaptiveTimeStep ? 1 : 0;
         return p;
     }
 
