@@ -38,7 +38,7 @@ __device__ __forceinline__ void for_neighbours(const SimConst& c, uint32_t i, co
     if (m <= (uint32_t)kNbCap) {
         for (uint32_t k = 0; k < m; ++k) {
             const uint32_t j = __ldg(nbr + nbr_index(i, k));
-            f(j, ldg4(pos + j));
+            if (j != i) f(j, ldg4(pos + j));  // the list records the particle itself
         }
     } else {
         for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {

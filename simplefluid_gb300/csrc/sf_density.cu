@@ -3,14 +3,16 @@
 // One thread per cell-sorted particle.  Poly6 density over the canonical
 // candidates; non-neighbours add an exact zero (fma(0, 0, s) == s), so the sum
 // is branch-free and bit-identical to summing neighbours only.  The pass also
-// evaluates the equation of state and records each particle's j != i
-// neighbours, in canonical order, for the force pass:
+// evaluates the equation of state and records each particle's neighbours
+// (itself included, in its canonical place) for the force pass:
 //   kEmitNone    no list (the force pass rescans the candidate cells);
 //   kEmitStaged  list staged in shared memory, written out in full lines;
 //   kEmitTile    list written directly.
 // Both list modes use the tile layout of nbr_index().  nbr_count[i] is the
 // full count; a count above kNbCap makes the force pass rescan that particle's
-// candidates instead of reading the list.
+// candidates instead of reading the list.  Recording the particle itself saves
+// a comparison per candidate; its pair terms in the force pass are exact
+// zeros (fma(w, v_i - v_i, a) == a, and the pressure term needs r > 0).
 #include "sf_device.cuh"
 
 namespace sf {
@@ -36,7 +38,7 @@ __global__ void __launch_bounds__(kBlockSize)
             const bool near = r2 < c.h2;
             const float q = near ? c.h2 - r2 : 0.f;
             s = fmaf(q * q, q, s);
-            if (kMode != kEmitNone && near && j != i) {
+            if (kMode != kEmitNone && near) {
                 if (cnt < kNbCap) {
                     if (kMode == kEmitStaged) s_nb[cnt][t] = j;
                     if (kMode == kEmitTile) nbr[nbr_index(i, cnt)] = j;

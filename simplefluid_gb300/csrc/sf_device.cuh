@@ -107,17 +107,11 @@ __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t
             const float g2 = fmaf(gz, gz, gy * gy);
             if (g2 >= c.prune_h2) continue;
             int lo = -kReach, hi = kReach;
-            if (kReach > 1) {
-                while (lo < 0) {
-                    const float gx = face_gap(ox, lo, c.cell_w[0], c.prune_margin);
-                    if (fmaf(gx, gx, g2) < c.prune_h2) break;
-                    ++lo;
-                }
-                while (hi > 0) {
-                    const float gx = face_gap(ox, hi, c.cell_w[0], c.prune_margin);
-                    if (fmaf(gx, gx, g2) < c.prune_h2) break;
-                    --hi;
-                }
+            if (kReach > 1) {  // drop the row's outermost cell on a side when it is out of reach
+                const float gl = face_gap(ox, -kReach, c.cell_w[0], c.prune_margin);
+                const float gh = face_gap(ox, kReach, c.cell_w[0], c.prune_margin);
+                if (fmaf(gl, gl, g2) >= c.prune_h2) lo = 1 - kReach;
+                if (fmaf(gh, gh, g2) >= c.prune_h2) hi = kReach - 1;
             }
             const int x0 = max(cx + lo, 0), x1 = min(cx + hi, c.n[0] - 1);
             const uint32_t row = c.cell_base + ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
@@ -150,7 +144,8 @@ __device__ __forceinline__ size_t nbr_index(uint32_t i, uint32_t k) {
     return ((size_t)(i / kNbTile) * kNbCap + k) * kNbTile + (i % kNbTile);
 }
 
-// Pair terms of particle i with neighbour j (j != i, |xi - xj| < h), in the
+// Pair terms of particle i with neighbour j (|xi - xj| < h; j == i adds exact
+// zeros), in the
 // oracle's operation order.
 struct PairAcc {
     float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
