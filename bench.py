@@ -52,7 +52,7 @@ STAGE_BYTES_PER_PARTICLE = {
     "scatter": 8 + 4 + 4,                    # read key+slot, cell start; write index
     "rank_gather": 8 + 8 + 24 + 24,          # read key, cell range; read pos+vel; write pos+vel
 }
-STAGE_BYTES_PER_CELL = {"scan_reduce": 4, "scan_tiles": 0, "scan_apply": 4 + 4 + 4}
+STAGE_BYTES_PER_CELL = {"scan": 4 + 4}  # read the cell histogram, write the cell table
 STEP_BYTES_PER_UPDATE = 213  # canonical whole-step figure (hash 20 + sort 16 + reorder 48 + cells 5 + density 20 + force 44 + integrate 60)
 
 WORKLOADS = {

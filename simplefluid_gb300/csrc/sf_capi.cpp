@@ -243,6 +243,7 @@ sf_status alloc_grid(sf_ctx* ctx) {
     SF_CUDA(cudaMalloc(&d.counts, pad * sizeof(uint32_t)));
     SF_CUDA(cudaMalloc(&d.cell_start, pad * sizeof(uint32_t)));
     SF_CUDA(cudaMalloc(&d.tile_sums, (size_t)d.ntiles * sizeof(uint32_t)));
+    SF_CUDA(cudaMemsetAsync(d.tile_sums, 0, (size_t)d.ntiles * sizeof(uint32_t), ctx->stream));
     SF_CUDA(cudaMemsetAsync(d.counts, 0, pad * sizeof(uint32_t), ctx->stream));
     SF_CUDA(cudaMemsetAsync(d.cell_start, 0, pad * sizeof(uint32_t), ctx->stream));
     return SF_OK;

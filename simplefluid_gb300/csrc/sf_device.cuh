@@ -70,6 +70,19 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {  // murmur3 finaliser
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+// Counting-sort histogram: the particle's arrival slot in its cell, and the
+// cell's scan tile total (one atomic per distinct tile per warp).  Call with
+// every live lane of the warp converged.
+__device__ __forceinline__ uint32_t count_in_cell(uint32_t key, uint32_t* __restrict__ counts,
+                                                  uint32_t* __restrict__ tile_sums) {
+    const uint32_t slot = atomicAdd(counts + key, 1u);
+    const unsigned mask = __activemask();
+    const uint32_t tile = key / (uint32_t)kScanTile;
+    const unsigned peers = __match_any_sync(mask, tile);
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(tile_sums + tile, (uint32_t)__popc(peers));
+    return slot;
+}
+
 // Lower bound, minus the pruning slack, of the axis distance from a point at
 // offset `off` inside its cell (width w) to the cell at offset d.
 __device__ __forceinline__ float face_gap(float off, int d, float w, float margin) {

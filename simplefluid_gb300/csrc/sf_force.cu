@@ -20,8 +20,8 @@ __global__ void __launch_bounds__(kBlockSize)
             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
             uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
             uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-            uint32_t* __restrict__ counts, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
-            float4* __restrict__ sums, FrameState* __restrict__ frame) {
+            uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot,
+            float4* __restrict__ acc_out, float4* __restrict__ sums, FrameState* __restrict__ frame) {
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     if (i >= n) return;
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kBlockSize)
     pos_out[i] = make_float4(x[0], x[1], x[2], xi.w);
     vel_out[i] = make_float4(v[0], v[1], v[2], 0.f);
     const uint32_t key = cell_key(c, x[0], x[1], x[2]);
-    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+    key_slot[i] = make_uint2(key, count_in_cell(key, counts, tile_sums));
     if (frame && c.adaptive) {
         // maxima of |v'|^2 and |a|^2 (non-negative floats order like their bits)
         const unsigned mask = __activemask();
@@ -108,6 +108,7 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
         float4* po = kIntegrate ? d.pos2 : nullptr;
         float4* vo = kIntegrate ? d.vel2 : nullptr;
         uint32_t* co = kIntegrate ? d.counts : nullptr;
+        uint32_t* ts = kIntegrate ? d.tile_sums : nullptr;
         uint2* ks = kIntegrate ? d.key_slot : nullptr;
         float4* ac = kIntegrate ? nullptr : d.accel;
         if (d.table) {
@@ -115,10 +116,10 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
                 k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>
                     <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.nbr,
                                                                      d.nbr_count, d.n, c, d.table, d.scene_off,
-                                                                     d.nscenes, po, vo, co, ks, ac, d.sums, nullptr);
+                                                                     d.nscenes, po, vo, co, ts, ks, ac, d.sums, nullptr);
         } else {
             k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ks,
+                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ts, ks,
                 ac, d.sums, kIntegrate ? d.frame : nullptr);
         }
     });

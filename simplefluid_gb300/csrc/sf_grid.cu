@@ -74,13 +74,13 @@ __global__ void k_store_aos(const float4* __restrict__ pos, const float4* __rest
 template <bool kBatched>
 __global__ void k_hash_count(const float4* __restrict__ pos, uint32_t n, SimConst c0, const SimConst* __restrict__ table,
                              const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t* __restrict__ counts,
-                             uint2* __restrict__ key_slot) {
+                             uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 p = pos[i];
     const uint32_t key = cell_key(c, p.x, p.y, p.z);
-    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
+    key_slot[i] = make_uint2(key, count_in_cell(key, counts, tile_sums));
 }
 
 template <bool kBatched>
@@ -123,47 +123,35 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint4* __restrict__ counts,
-                                                              uint32_t* __restrict__ tile_sums) {
+// Exclusive scan of the cell histogram into the cell table.  Block b scans
+// tile b (kScanTile cells) and adds the totals of tiles 0..b-1, which the
+// histogram atomics accumulated in tile_sums, so one kernel does the whole scan.
+__global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__ counts,
+                                                       const uint32_t* __restrict__ tile_sums,
+                                                       uint4* __restrict__ cell_start) {
     __shared__ uint32_t total;
-    const uint4 q = counts[(size_t)blockIdx.x * kScanThreads + threadIdx.x];
-    block_exclusive(q.x + q.y + q.z + q.w, &total);
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(uint32_t* __restrict__ tile_sums, uint32_t ntiles) {
-    __shared__ uint32_t total;
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < ntiles; base += kScanThreads) {
-        const uint32_t t = base + threadIdx.x;
-        const uint32_t v = t < ntiles ? tile_sums[t] : 0u;
-        const uint32_t ex = block_exclusive(v, &total);
-        if (t < ntiles) tile_sums[t] = carry + ex;
-        carry += total;
-        __syncthreads();
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint4* __restrict__ counts,
-                                                             const uint32_t* __restrict__ tile_sums,
-                                                             uint4* __restrict__ cell_start) {
-    __shared__ uint32_t total;
+    uint32_t before = 0;
+    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += kScanThreads) before += tile_sums[t];
+    block_exclusive(before, &total);
+    const uint32_t offset = total;
     const size_t t = (size_t)blockIdx.x * kScanThreads + threadIdx.x;
     const uint4 q = counts[t];
-    const uint32_t ex = block_exclusive(q.x + q.y + q.z + q.w, &total) + tile_sums[blockIdx.x];
+    const uint32_t ex = block_exclusive(q.x + q.y + q.z + q.w, &total) + offset;
     cell_start[t] = make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
 }
 
 // ---------------------------------------------------------------- reorder
-// Buckets indices by cell and clears the occupied cells' counters for the next
-// step (only occupied cells were counted, so this leaves all counters zero).
+// Buckets indices by cell and clears the occupied cells' counters and their
+// tiles' totals for the next step (only those were counted, so this leaves
+// every counter zero).
 __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start, uint32_t n,
-                          uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts) {
+                          uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 ks = key_slot[i];
     tmp[cell_start[ks.x] + ks.y] = i;
     counts[ks.x] = 0u;
+    tile_sums[ks.x / (uint32_t)kScanTile] = 0u;
 }
 
 __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start,
@@ -229,9 +217,10 @@ void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, cons
     if (!n) return;
     if (d.table)
         k_hash_count<true><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, d.table, d.scene_off, d.nscenes, counts,
-                                                                  key_slot);
+                                                                  d.tile_sums, key_slot);
     else
-        k_hash_count<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, counts, key_slot);
+        k_hash_count<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, counts, d.tile_sums,
+                                                                   key_slot);
 }
 
 void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
@@ -243,26 +232,14 @@ void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimC
         k_keys<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, keys);
 }
 
-static void launch_scan_reduce(DeviceState& d, cudaStream_t s) {
-    k_scan_reduce<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums);
-}
-static void launch_scan_tiles(DeviceState& d, cudaStream_t s) {
-    k_scan_tiles<<<1, kScanThreads, 0, s>>>(d.tile_sums, d.ntiles);
-}
-static void launch_scan_apply(DeviceState& d, cudaStream_t s) {
-    k_scan_apply<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
-                                                   reinterpret_cast<uint4*>(d.cell_start));
-}
-
 void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
-    launch_scan_reduce(d, s);
-    launch_scan_tiles(d, s);
-    launch_scan_apply(d, s);
+    k_scan<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
+                                             reinterpret_cast<uint4*>(d.cell_start));
 }
 
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    cudaStream_t s) {
-    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts);
+                    uint32_t* tile_sums, cudaStream_t s) {
+    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts, tile_sums);
 }
 
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
@@ -290,22 +267,19 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
 
 void enqueue_sort_tail(DeviceState& d, cudaStream_t s) {
     launch_scan_cells(d, d.n, s);
-    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s);
+    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, s);
     launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
 }
 
-const char* const kStageNames[kNumStages] = {"density",    "force_integrate", "scan_reduce", "scan_tiles",
-                                             "scan_apply", "scatter",         "rank_gather"};
+const char* const kStageNames[kNumStages] = {"density", "force_integrate", "scan", "scatter", "rank_gather"};
 
 void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s) {
     switch (stage) {
         case 0: launch_density(d, c, s); break;
         case 1: launch_force_integrate(d, c, s); break;
-        case 2: launch_scan_reduce(d, s); break;
-        case 3: launch_scan_tiles(d, s); break;
-        case 4: launch_scan_apply(d, s); break;
-        case 5: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s); break;
-        case 6: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
+        case 2: launch_scan_cells(d, d.n, s); break;
+        case 3: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, s); break;
+        case 4: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
         default: break;
     }
 }

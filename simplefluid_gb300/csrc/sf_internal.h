@@ -88,8 +88,9 @@ struct DeviceState {
     // grid
     uint32_t ncells = 0, ncells_pad = 0;
     uint32_t* counts = nullptr;      // ncells_pad, zero between steps
+    // per scan tile (kScanTile cells): particles counted in it, zero between steps
     uint32_t* cell_start = nullptr;  // ncells + 1
-    uint32_t* tile_sums = nullptr;   // one per scan tile
+    uint32_t* tile_sums = nullptr;
     uint32_t ntiles = 0;
     // batches of independent scenes (null for a single scene): per-scene
     // constants and the first particle index of each scene (nscenes + 1)
@@ -120,7 +121,7 @@ void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, cons
                        uint2* key_slot, cudaStream_t s);
 void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    cudaStream_t s);
+                    uint32_t* tile_sums, cudaStream_t s);
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
                         const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s);
 void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
@@ -140,7 +141,7 @@ void enqueue_sort_tail(DeviceState& d, cudaStream_t s);
 void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);
 
 // The sub-step as separately launchable stages (for per-stage timing).
-constexpr uint32_t kNumStages = 7;
+constexpr uint32_t kNumStages = 5;
 extern const char* const kStageNames[kNumStages];
 void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream_t s);
 

@@ -126,9 +126,10 @@ int noalloc_density(const sf_params& p, const SimConst& c, const float* d_pos_xy
     d.ncells = c.ncells;
     d.ncells_pad = (uint32_t)(((uint64_t)c.ncells + 1 + kScanTile - 1) / kScanTile * kScanTile);
     d.ntiles = d.ncells_pad / kScanTile;
-    // The counters must start at zero; a previous call normally leaves them
-    // zero, but an interrupted one may not.
+    // The counters (per cell and per scan tile) must start at zero; a previous
+    // call normally leaves them zero, but an interrupted one may not.
     e = cudaMemsetAsync(d.counts, 0, (size_t)d.ncells_pad * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.tile_sums, 0, (size_t)d.ntiles * sizeof(uint32_t), stream);
     if (e != cudaSuccess) {
         *why = "sf_density_noalloc: clearing the cell counters failed";
         return SF_ERR_CUDA;
