@@ -263,6 +263,21 @@ def measure_adjoint(args) -> dict:
                       "adjoint includes the checkpointed forward recompute"}
 
 
+def aggregate_over_ranks(dist, local_ms: float, local_units: int):
+    """Whole-job timing of replicas: the slowest rank's time and the units all
+    ranks processed (weak scaling: every rank runs its own copy of the
+    workload).  `dist` is torch.distributed (initialised) or None."""
+    if dist is None:
+        return local_ms, local_units
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_ms], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(local_units)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(round(float(u.item())))
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
@@ -320,12 +335,7 @@ def run_ours(args, workload):
             dist.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return aggregate_over_ranks(dist, x, 0)[0]
 
     # warm-up
     C.check(lib.sf_step(ctx, max(args.warmup, 3)))
@@ -342,8 +352,8 @@ def run_ours(args, workload):
         warm_ms = ctypes.c_float()
         C.check(lib.sf_step_timed(ctx, args.steps, 0, ctypes.byref(warm_ms), None))
     barrier()
-    t_ms = max_over_ranks(total_ms.value)
-    value = ws * n * args.steps / (t_ms * 1e-3)
+    t_ms, units = aggregate_over_ranks(dist, total_ms.value, n * args.steps)
+    value = units / (t_ms * 1e-3)
 
     # per-stage device times over K profiled (non-graph) steps
     nst = lib.sf_stage_count()
