@@ -71,16 +71,19 @@ __global__ void k_store_aos(const float4* __restrict__ pos, const float4* __rest
 }
 
 // ---------------------------------------------------------------- hashing
+// Histogram of an uploaded (not cell-sorted) state.  Its lanes hit scattered
+// scan tiles, so the tile totals come from a separate reduction instead of
+// per-particle tile atomics.
 template <bool kBatched>
 __global__ void k_hash_count(const float4* __restrict__ pos, uint32_t n, SimConst c0, const SimConst* __restrict__ table,
                              const uint32_t* __restrict__ scene_off, uint32_t nscenes, uint32_t* __restrict__ counts,
-                             uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot) {
+                             uint2* __restrict__ key_slot) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 p = pos[i];
     const uint32_t key = cell_key(c, p.x, p.y, p.z);
-    key_slot[i] = make_uint2(key, count_in_cell(key, counts, tile_sums));
+    key_slot[i] = make_uint2(key, atomicAdd(counts + key, 1u));
 }
 
 template <bool kBatched>
@@ -123,6 +126,15 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
     return r;
 }
 
+// Tile totals of the cell histogram (one block per scan tile).
+__global__ void __launch_bounds__(kScanThreads) k_tile_totals(const uint4* __restrict__ counts,
+                                                              uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t total;
+    const uint4 q = counts[(size_t)blockIdx.x * kScanThreads + threadIdx.x];
+    block_exclusive(q.x + q.y + q.z + q.w, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
 // Exclusive scan of the cell histogram into the cell table.  Block b scans
 // tile b (kScanTile cells) and adds the totals of tiles 0..b-1, which the
 // histogram atomics accumulated in tile_sums, so one kernel does the whole scan.
@@ -141,17 +153,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__
 }
 
 // ---------------------------------------------------------------- reorder
-// Buckets indices by cell and clears the occupied cells' counters and their
-// tiles' totals for the next step (only those were counted, so this leaves
-// every counter zero).
+// Buckets indices by cell and clears the occupied cells' counters for the
+// next step (only those were counted, so this leaves every counter zero).
 __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start, uint32_t n,
-                          uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums) {
+                          uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 ks = key_slot[i];
     tmp[cell_start[ks.x] + ks.y] = i;
     counts[ks.x] = 0u;
-    tile_sums[ks.x / (uint32_t)kScanTile] = 0u;
 }
 
 __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start,
@@ -217,10 +227,10 @@ void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, cons
     if (!n) return;
     if (d.table)
         k_hash_count<true><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, d.table, d.scene_off, d.nscenes, counts,
-                                                                  d.tile_sums, key_slot);
+                                                                  key_slot);
     else
-        k_hash_count<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, counts, d.tile_sums,
-                                                                   key_slot);
+        k_hash_count<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, c, nullptr, nullptr, 0, counts, key_slot);
+    k_tile_totals<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(counts), d.tile_sums);
 }
 
 void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
@@ -237,9 +247,12 @@ void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
                                              reinterpret_cast<uint4*>(d.cell_start));
 }
 
+// Buckets indices by cell and clears the counters; the scan-tile totals (a
+// few KB) are cleared with one memset.
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    uint32_t* tile_sums, cudaStream_t s) {
-    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts, tile_sums);
+                    uint32_t* tile_sums, uint32_t ntiles, cudaStream_t s) {
+    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts);
+    cudaMemsetAsync(tile_sums, 0, (size_t)ntiles * sizeof(uint32_t), s);
 }
 
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
@@ -267,7 +280,7 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
 
 void enqueue_sort_tail(DeviceState& d, cudaStream_t s) {
     launch_scan_cells(d, d.n, s);
-    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, s);
+    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, d.ntiles, s);
     launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
 }
 
@@ -278,7 +291,7 @@ void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream
         case 0: launch_density(d, c, s); break;
         case 1: launch_force_integrate(d, c, s); break;
         case 2: launch_scan_cells(d, d.n, s); break;
-        case 3: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, s); break;
+        case 3: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, d.ntiles, s); break;
         case 4: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
         default: break;
     }

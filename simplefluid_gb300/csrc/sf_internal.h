@@ -117,11 +117,12 @@ void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* id
 void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, uint32_t* ids,
                          cudaStream_t s);
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s);
+// Cell keys and histogram of an uploaded state, and its scan-tile totals.
 void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,
                        uint2* key_slot, cudaStream_t s);
 void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    uint32_t* tile_sums, cudaStream_t s);
+                    uint32_t* tile_sums, uint32_t ntiles, cudaStream_t s);
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
                         const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s);
 void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
