@@ -140,6 +140,42 @@ SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint3
 /* getNumParticles() */
 SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out);
 
+/* ---- particle state in device memory (no host round trip) ----------------
+ * The same state transfers with AoS float3 arrays that live in device memory
+ * of the context's GPU (cudaMalloc'd, or a framework tensor's storage).  Both
+ * are ordered on the context's stream and do not wait on the host.  `other`
+ * is the caller's cudaStream_t (as void*, NULL for none; the default stream
+ * is cudaStreamLegacy or cudaStreamPerThread, not NULL): set_state waits for
+ * the work already queued on it before reading, and get_state makes work
+ * queued on it afterwards wait for the written arrays.  A pointer that is not
+ * device memory of this GPU is rejected with SF_ERR_INVALID_ARGUMENT. */
+SF_API sf_status sf_set_state_device(sf_ctx* ctx, const float* d_pos_xyz, const float* d_vel_xyz, uint32_t n,
+                                     void* other);
+SF_API sf_status sf_get_state_device(sf_ctx* ctx, float* d_pos_xyz, float* d_vel_xyz, uint32_t n, void* other);
+
+/* Device views of the solver's working arrays, in its cell-sorted order:
+ *   pos4      float4 per particle: x, y, z, and in w the bit pattern of the
+ *             particle's caller index (uint32);
+ *   vel4      float4 per particle: vx, vy, vz, 0;
+ *   rho       density of the last density pass;
+ *   p_inv_rho float2 per particle: pressure and 1/rho of that pass;
+ *   cell_start ncells + 1 entries: the particles of cell c are
+ *             [cell_start[c], cell_start[c+1]).
+ * The pointers stay valid until the particle count changes or the context is
+ * destroyed; their contents change with every step.  Reads must be ordered
+ * after the context's stream (`stream`). */
+typedef struct sf_device_view {
+    const float* pos4;
+    const float* vel4;
+    const float* rho;
+    const float* p_inv_rho;
+    const uint32_t* cell_start;
+    uint32_t n;
+    uint32_t ncells;
+    void* stream;
+} sf_device_view;
+SF_API sf_status sf_device_state(sf_ctx* ctx, sf_device_view* view);
+
 /* ---- stepping: makeReady() / advanceFrame() ----------------------------- */
 /* Build the uniform grid, sort the particles and capture the step graph. */
 SF_API sf_status sf_make_ready(sf_ctx* ctx);

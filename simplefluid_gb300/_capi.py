@@ -97,6 +97,13 @@ class sf_render_params(ctypes.Structure):
     ]
 
 
+class sf_device_view(ctypes.Structure):
+    """Mirror of ``struct sf_device_view`` (include/sf_capi.h)."""
+
+    _fields_ = [("pos4", c_void_p), ("vel4", c_void_p), ("rho", c_void_p), ("p_inv_rho", c_void_p),
+                ("cell_start", c_void_p), ("n", c_uint32), ("ncells", c_uint32), ("stream", c_void_p)]
+
+
 class SFError(RuntimeError):
     """Raised when a C-ABI call returns a non-zero sf_status."""
 
@@ -121,6 +128,9 @@ PROTOTYPES = {
     "sf_get_params": (c_int32, [c_void_p, _P(sf_params)]),
     "sf_set_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
     "sf_get_state": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "sf_set_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
+    "sf_get_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
+    "sf_device_state": (c_int32, [c_void_p, _P(sf_device_view)]),
     "sf_get_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
     "sf_make_ready": (c_int32, [c_void_p]),
     "sf_advance_frame": (c_int32, [c_void_p, _P(c_float)]),

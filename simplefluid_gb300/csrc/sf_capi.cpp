@@ -282,9 +282,11 @@ sf_status check_launch(const char* what) {
 }
 
 // Upload n particles (device AoS staging already filled) and cell-sort them.
-sf_status sort_uploaded(sf_ctx* ctx) {
+// Load a caller-order AoS state from device arrays (vel3 NULL: at rest) and
+// sort it into the cell order.
+sf_status sort_uploaded(sf_ctx* ctx, const float* pos3, const float* vel3) {
     sf::DeviceState& d = ctx->d;
-    sf::launch_load_aos(d.io, d.io + 3 * (size_t)d.n, d.n, d.pos2, d.vel2, ctx->stream);
+    sf::launch_load_aos(pos3, vel3, d.n, d.pos2, d.vel2, ctx->stream);
     sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
     sf::enqueue_sort_tail(d, ctx->stream);
     if (ctx->frame) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
@@ -680,12 +682,8 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
     float* io = ctx->d.io;
     const size_t bytes = (size_t)n * 3 * sizeof(float);
     SF_TRY(copy_in(ctx, io, pos_xyz, bytes));
-    if (vel_xyz) {
-        SF_TRY(copy_in(ctx, io + 3 * (size_t)n, vel_xyz, bytes));
-    } else {
-        SF_CUDA(cudaMemsetAsync(io + 3 * (size_t)n, 0, bytes, ctx->stream));
-    }
-    SF_TRY(sort_uploaded(ctx));
+    if (vel_xyz) SF_TRY(copy_in(ctx, io + 3 * (size_t)n, vel_xyz, bytes));
+    SF_TRY(sort_uploaded(ctx, io, vel_xyz ? io + 3 * (size_t)n : nullptr));
     // The caller may reuse its buffers once this returns.
     SF_CUDA(cudaStreamSynchronize(ctx->stream));
     return SF_OK;
@@ -710,6 +708,77 @@ SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out) {
     SF_TRY(need_ctx(ctx));
     if (!n_out) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
     *n_out = ctx->d.n;
+    return SF_OK;
+}
+
+namespace {
+
+// Device memory of the context's GPU (plain or managed).
+sf_status need_device_array(const sf_ctx* ctx, const void* p, const char* what) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SF_ERR_INVALID_ARGUMENT, std::string(what) + " is not a CUDA pointer");
+    }
+    if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != ctx->device)
+        return fail(SF_ERR_INVALID_ARGUMENT, std::string(what) + " is not device memory of the context's GPU");
+    return SF_OK;
+}
+
+// Order `waiter` after the work queued so far on `signaller`.
+sf_status stream_after(cudaStream_t waiter, cudaStream_t signaller) {
+    if (!signaller || signaller == waiter) return SF_OK;
+    cudaEvent_t ev;
+    SF_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, signaller);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(waiter, ev, 0);
+    cudaEventDestroy(ev);
+    SF_CUDA(e);
+    return SF_OK;
+}
+
+}  // namespace
+
+SF_API sf_status sf_set_state_device(sf_ctx* ctx, const float* d_pos_xyz, const float* d_vel_xyz, uint32_t n,
+                                     void* other) {
+    SF_TRY(need_ctx(ctx));
+    if (n && !d_pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null positions");
+    SF_TRY(set_device(ctx));
+    if (n) SF_TRY(need_device_array(ctx, d_pos_xyz, "positions"));
+    if (n && d_vel_xyz) SF_TRY(need_device_array(ctx, d_vel_xyz, "velocities"));
+    const bool resized = n != ctx->d.n;
+    SF_TRY(alloc_particles(ctx, n));
+    if (resized) drop_graph(ctx);
+    ctx->d.n = n;
+    ctx->sorted = false;
+    if (n == 0) return SF_OK;
+    SF_TRY(stream_after(ctx->stream, (cudaStream_t)other));
+    return sort_uploaded(ctx, d_pos_xyz, d_vel_xyz);
+}
+
+SF_API sf_status sf_get_state_device(sf_ctx* ctx, float* d_pos_xyz, float* d_vel_xyz, uint32_t n, void* other) {
+    SF_TRY(need_sorted(ctx));
+    if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
+    SF_TRY(set_device(ctx));
+    if (n && d_pos_xyz) SF_TRY(need_device_array(ctx, d_pos_xyz, "positions"));
+    if (n && d_vel_xyz) SF_TRY(need_device_array(ctx, d_vel_xyz, "velocities"));
+    sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, d_pos_xyz, d_vel_xyz, ctx->stream);
+    SF_TRY(check_launch("store state"));
+    return stream_after((cudaStream_t)other, ctx->stream);
+}
+
+SF_API sf_status sf_device_state(sf_ctx* ctx, sf_device_view* view) {
+    SF_TRY(need_sorted(ctx));
+    if (!view) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    const sf::DeviceState& d = ctx->d;
+    view->pos4 = reinterpret_cast<const float*>(d.pos);
+    view->vel4 = reinterpret_cast<const float*>(d.vel);
+    view->rho = d.rho;
+    view->p_inv_rho = reinterpret_cast<const float*>(d.pr);
+    view->cell_start = d.cell_start;
+    view->n = d.n;
+    view->ncells = d.ncells;
+    view->stream = (void*)ctx->stream;
     return SF_OK;
 }
 

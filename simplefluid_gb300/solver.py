@@ -31,6 +31,34 @@ def _vp(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(c_void_p)
 
 
+def _cuda_array(arr, what: str):
+    """(device pointer, n) of an (n, 3) float32 C-contiguous CUDA array."""
+    try:
+        cai = arr.__cuda_array_interface__
+    except AttributeError:
+        raise TypeError(f"{what} must expose __cuda_array_interface__ (a CUDA array)") from None
+    shape = tuple(cai["shape"])
+    if cai["typestr"] != "<f4" or len(shape) != 2 or shape[1] != 3:
+        raise ValueError(f"{what} must be an (n, 3) float32 array")
+    strides = cai.get("strides")
+    if strides is not None and tuple(strides) != (12, 4):
+        raise ValueError(f"{what} must be C-contiguous")
+    ptr = int(cai["data"][0])
+    return (c_void_p(ptr) if ptr else None), int(shape[0])
+
+
+def _stream_handle(stream, arr=None):
+    """cudaStream_t of `stream` (an int, or an object with .cuda_stream), else
+    the stream named by a version-3 __cuda_array_interface__, else None.  The
+    default stream (handle 0) is passed as cudaStreamLegacy (1)."""
+    if stream is None and arr is not None:
+        stream = getattr(arr, "__cuda_array_interface__", {}).get("stream")
+    if stream is None:
+        return None
+    handle = int(getattr(stream, "cuda_stream", stream))
+    return c_void_p(handle if handle else 1)
+
+
 @dataclass
 class SPHParameters:
     """Mirror of ``SPHParameters<float>``; defaults are the 16k dambreak workload."""
@@ -165,6 +193,43 @@ class SPHSolver:
         vel = np.empty((n, 3), np.float32)
         C.check(self._lib.sf_get_state(self._ctx, _vp(pos), _vp(vel), n))
         return pos, vel
+
+    # -- state in device memory --------------------------------------------------
+    # Arrays are (n, 3) float32, C-contiguous, in device memory of the solver's
+    # GPU, given as any object exposing __cuda_array_interface__ (a torch CUDA
+    # tensor, for one).  `stream` is the caller's stream (a cudaStream_t as int,
+    # or an object with a ``cuda_stream`` attribute such as torch.cuda.Stream):
+    # the solver reads after the work queued on it, and work queued on it after
+    # getStateDevice sees the written arrays.
+    def setParticlesDevice(self, particles, velocity=None, stream=None) -> None:
+        pptr, n = _cuda_array(particles, "particles")
+        vptr = None
+        if velocity is not None:
+            vptr, nv = _cuda_array(velocity, "velocity")
+            if nv != n:
+                raise ValueError("velocity must have the same shape as particles")
+        C.check(self._lib.sf_set_state_device(self._ctx, pptr, vptr, n, _stream_handle(stream, particles)))
+        self._n = n
+
+    def getStateDevice(self, particles=None, velocity=None, stream=None) -> None:
+        """Write the state, in the caller's particle order, into device arrays."""
+        n = self.getNumParticles()
+        ptrs = []
+        for arr, what in ((particles, "particles"), (velocity, "velocity")):
+            if arr is None:
+                ptrs.append(None)
+                continue
+            ptr, na = _cuda_array(arr, what)
+            if na != n:
+                raise ValueError(f"{what} must hold {n} particles")
+            ptrs.append(ptr)
+        C.check(self._lib.sf_get_state_device(self._ctx, ptrs[0], ptrs[1], n, _stream_handle(stream, particles)))
+
+    def deviceState(self) -> "C.sf_device_view":
+        """Device pointers to the cell-sorted working arrays (sf_device_view)."""
+        v = C.sf_device_view()
+        C.check(self._lib.sf_device_state(self._ctx, byref(v)))
+        return v
 
     # -- stepping ------------------------------------------------------------
     def makeReady(self) -> None:
