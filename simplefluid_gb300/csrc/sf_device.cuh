@@ -98,8 +98,65 @@ __device__ __forceinline__ float face_gap(float off, int d, float w, float margi
 // Rows and end cells whose nearest face is provably farther than h (by a
 // margin that covers the rounding of cell assignment) are skipped: they hold
 // no neighbour, so skipping them changes no sum and no list.
+// This form unrolls the dy rows over per-particle gap tables (fastest where
+// the walk is the kernel's main loop); for_candidates_rolled below is the
+// same walk in less code and fewer registers, for kernels where it is a rare
+// path (the force pass's list-overflow rescan).
 template <int kReach, typename F>
 __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
+                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
+    const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
+    const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
+    const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
+    const float ox = (x - c.bmin[0]) - (float)cx * c.cell_w[0];  // positions inside the cell
+    const float oy = (y - c.bmin[1]) - (float)cy * c.cell_w[1];
+    const float oz = (z - c.bmin[2]) - (float)cz * c.cell_w[2];
+    const uint32_t n0 = (uint32_t)c.n[0], n1 = (uint32_t)c.n[1];
+    // Per row offset dy: the squared gap (infinite outside the grid).  Per row
+    // end: the squared gap of the outermost cell, which is dropped when out
+    // of reach.  Rounding of these sums is far inside prune_h2's slack.
+    float gy2[2 * kReach + 1];
+#pragma unroll
+    for (int d = -kReach; d <= kReach; ++d) {
+        const float g = face_gap(oy, d, c.cell_w[1], c.prune_margin);
+        gy2[d + kReach] = (cy + d < 0 || cy + d >= c.n[1]) ? __int_as_float(0x7f800000) : g * g;
+    }
+    float glo2 = 0.f, ghi2 = 0.f;
+    if (kReach > 1) {
+        const float gl = face_gap(ox, -kReach, c.cell_w[0], c.prune_margin);
+        const float gh = face_gap(ox, kReach, c.cell_w[0], c.prune_margin);
+        glo2 = gl * gl;
+        ghi2 = gh * gh;
+    }
+    const int xa = max(cx - kReach, 0), xb = min(cx + kReach, c.n[0] - 1);
+    const int xa1 = max(cx - kReach + 1, 0), xb1 = min(cx + kReach - 1, c.n[0] - 1);
+#pragma unroll 1
+    for (int dz = -kReach; dz <= kReach; ++dz) {
+        const int zz = cz + dz;
+        if (zz < 0 || zz >= c.n[2]) continue;
+        const float gz = face_gap(oz, dz, c.cell_w[2], c.prune_margin);
+        const float gz2 = gz * gz;
+        if (gz2 >= c.prune_h2) continue;
+        // cell table of row (zz, cy); rows dy are n0 entries apart
+        const uint32_t* plane = cs + c.cell_base + ((uint32_t)zz * n1 + (uint32_t)cy) * n0;
+#pragma unroll
+        for (int dy = -kReach; dy <= kReach; ++dy) {
+            const float g2 = gz2 + gy2[dy + kReach];
+            if (g2 >= c.prune_h2) continue;
+            const int x0 = (kReach > 1 && g2 + glo2 >= c.prune_h2) ? xa1 : xa;
+            const int x1 = (kReach > 1 && g2 + ghi2 >= c.prune_h2) ? xb1 : xb;
+            const uint32_t* row = plane + dy * (int)n0;
+            const uint32_t b = __ldg(row + x0), e = __ldg(row + x1 + 1);
+#pragma unroll 1
+            for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+        }
+    }
+}
+
+// The candidate walk above with both row loops rolled and the gaps computed
+// per row.
+template <int kReach, typename F>
+__device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const uint32_t* __restrict__ cs,
                                                const float4* __restrict__ pos, float x, float y, float z, F&& f) {
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
     const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kBlockSize)
             pair_terms(c, xi, vi, pri.x, ldg4(pos + j), __ldg(pr + j), ldg4(vel + j), a);
         }
     } else {
-        for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+        for_candidates_rolled<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             if (j == i) return;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)

@@ -110,7 +110,7 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-// ---- kernel launchers (sf_kernels.cu); all enqueue on `s` ---------------
+// ---- kernel launchers (sf_grid.cu, sf_density.cu, sf_force.cu); all enqueue on `s`
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
 void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* ids, uint32_t n, float4* pos,
                         float4* vel, cudaStream_t s);
