@@ -139,16 +139,22 @@ __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t
         if (gz2 >= c.prune_h2) continue;
         // cell table of row (zz, cy); rows dy are n0 entries apart
         const uint32_t* plane = cs + c.cell_base + ((uint32_t)zz * n1 + (uint32_t)cy) * n0;
+        // the plane's row ranges, loaded together (empty for rows out of reach)
+        uint32_t rb[2 * kReach + 1], re[2 * kReach + 1];
 #pragma unroll
         for (int dy = -kReach; dy <= kReach; ++dy) {
             const float g2 = gz2 + gy2[dy + kReach];
-            if (g2 >= c.prune_h2) continue;
             const int x0 = (kReach > 1 && g2 + glo2 >= c.prune_h2) ? xa1 : xa;
             const int x1 = (kReach > 1 && g2 + ghi2 >= c.prune_h2) ? xb1 : xb;
             const uint32_t* row = plane + dy * (int)n0;
-            const uint32_t b = __ldg(row + x0), e = __ldg(row + x1 + 1);
+            const bool live = g2 < c.prune_h2;
+            rb[dy + kReach] = live ? __ldg(row + x0) : 0u;
+            re[dy + kReach] = live ? __ldg(row + x1 + 1) : 0u;
+        }
+#pragma unroll
+        for (int dy = 0; dy <= 2 * kReach; ++dy) {
 #pragma unroll 1
-            for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+            for (uint32_t j = rb[dy]; j < re[dy]; ++j) f(j, ldg4(pos + j));
         }
     }
 }

@@ -6,9 +6,10 @@
 // where the list overflowed or no list was recorded — then, in the stepping
 // variant, symplectic Euler, the box clamp with restitution and the next
 // step's cell key and arrival slot (the counting sort's histogram).
-// kPrefetch neighbours are gathered before their terms are added, so the
-// dependent index -> data loads overlap; the terms are still added in list
-// order, which keeps the sum bit-identical.
+// kPrefetch neighbours are gathered before their terms are added, and the
+// next kPrefetch list indices are loaded while they are, so the dependent
+// index -> data loads of consecutive batches overlap; the terms are still
+// added in list order, which keeps the sum bit-identical.
 #include "sf_device.cuh"
 
 namespace sf {
@@ -31,13 +32,21 @@ __global__ void __launch_bounds__(kBlockSize)
     PairAcc a;
     const uint32_t cnt = kUseList ? nbr_count[i] : 0xffffffffu;
     if (cnt <= (uint32_t)kNbCap) {
+        const uint32_t* lst = nbr + nbr_index(i, 0);  // slot k at lst[k * kNbTile]
+        uint32_t jn[kPrefetch];
+#pragma unroll
+        for (int u = 0; u < kPrefetch; ++u) jn[u] = __ldg(lst + (size_t)u * kNbTile);
         uint32_t k = 0;
         for (; k + kPrefetch <= cnt; k += kPrefetch) {
             uint32_t j[kPrefetch];
             float4 xj[kPrefetch], vj[kPrefetch];
             float2 pj[kPrefetch];
 #pragma unroll
-            for (int u = 0; u < kPrefetch; ++u) j[u] = __ldg(nbr + nbr_index(i, k + u));
+            for (int u = 0; u < kPrefetch; ++u) {
+                j[u] = jn[u];
+                // the next batch's indices (slots past the count hold stale values, unused)
+                jn[u] = __ldg(lst + (size_t)min(k + kPrefetch + u, (uint32_t)kNbCap - 1) * kNbTile);
+            }
 #pragma unroll
             for (int u = 0; u < kPrefetch; ++u) {
                 xj[u] = ldg4(pos + j[u]);
