@@ -102,9 +102,11 @@ __device__ __forceinline__ float face_gap(float off, int d, float w, float margi
 // the walk is the kernel's main loop); for_candidates_rolled below is the
 // same walk in less code and fewer registers, for kernels where it is a rare
 // path (the force pass's list-overflow rescan).
-template <int kReach, typename F>
-__device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
-                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
+// for_candidate_rows calls g(b, e) with the sorted index range [b, e) of each
+// candidate row in that order (ranges of rows out of reach are empty).
+template <int kReach, typename G>
+__device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint32_t* __restrict__ cs, float x,
+                                                   float y, float z, G&& g) {
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
     const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
     const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
@@ -152,11 +154,17 @@ __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t
             re[dy + kReach] = live ? __ldg(row + x1 + 1) : 0u;
         }
 #pragma unroll
-        for (int dy = 0; dy <= 2 * kReach; ++dy) {
-#pragma unroll 1
-            for (uint32_t j = rb[dy]; j < re[dy]; ++j) f(j, ldg4(pos + j));
-        }
+        for (int dy = 0; dy <= 2 * kReach; ++dy) g(rb[dy], re[dy]);
     }
+}
+
+template <int kReach, typename F>
+__device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
+                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
+    for_candidate_rows<kReach>(c, cs, x, y, z, [&](uint32_t b, uint32_t e) {
+#pragma unroll 1
+        for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+    });
 }
 
 // The candidate walk above with both row loops rolled and the gaps computed
