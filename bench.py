@@ -209,8 +209,23 @@ def measure_batched(args) -> dict:
     finally:
         for c in ctxs:
             c.close()
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the CPU oracle over the scenes one after another, on a sample of them
+        ups = secs = 0.0
+        threads = 1
+        sample = range(0, len(params), 32)
+        for s in sample:
+            pp = SPHParameters.from_c(params[s])
+            pp.cellsPerH = K
+            rate, st, threads = cpu_oracle_rate(pos[off[s]:off[s + 1]], pp, args.cpu_seconds / 8, 20)
+            ups += (off[s + 1] - off[s]) * st
+            secs += (off[s + 1] - off[s]) * st / rate
+        cpu = {"value": ups / secs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"scenes {list(sample)} one after another, up to 20 sub-steps each (after 1 warm-up)"}
     return {"value": batched, "unit": UNIT, "scenes": len(params), "particles": n, "steps": steps,
             "sequential_value": seq, "ratio_vs_sequential": batched / seq, "interleaved_streams_value": rr,
+            "cpu_baseline": cpu,
             "autotuned": {"cells_per_h": K, "list_mode": tune.list_mode, "density_block": tune.density_block,
                           "force_block": tune.force_block, "prefetch": tune.prefetch, "seconds": tune_s},
             "timing": "batched: CUDA events over the graph-replayed steps (warm L2); sequential and interleaved: "
@@ -261,6 +276,38 @@ def measure_adjoint(args) -> dict:
             "dloss_dviscosity": float(dmu), "dloss_dstiffness": float(dk),
             "timing": "forward: CUDA events over graph-replayed steps; others: wall clock, best of 3, "
                       "adjoint includes the checkpointed forward recompute"}
+
+
+def measure_other_workloads(args, skip: str) -> dict:
+    """The other single-scene workloads on the GPU (graph-replayed sub-steps,
+    CUDA events, L2 flushed before every step) beside the CPU oracle on the
+    host cores (a time-bounded sample from the initial state)."""
+    from simplefluid_gb300 import SPHSolver, scene_positions
+    from simplefluid_gb300 import _capi as C
+    lib = C.load()
+    plan = {"dambreak_16k": 500, "sphere_pool": 100}
+    out = {}
+    for wl, steps in plan.items():
+        if wl == skip:
+            continue
+        prm = make_params(wl)
+        pos = scene_positions(prm, prm.scene)
+        n = int(pos.shape[0])
+        with SPHSolver(prm) as s:
+            s.setParticles(pos)
+            s.makeReady()
+            s.step(3)
+            s.setParticles(pos)
+            ms = ctypes.c_float()
+            C.check(lib.sf_step_timed(s.handle, steps, FLUSH_BYTES, ctypes.byref(ms), None))
+        rec = {"particles": n, "steps": steps, "value": n * steps / (ms.value * 1e-3), "unit": UNIT,
+               "ms_per_step": ms.value / steps}
+        if not args.no_cpu_baseline:
+            rate, csteps, threads = cpu_oracle_rate(pos, prm, args.cpu_seconds / 3, steps)
+            rec["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": f"{csteps} sub-steps from the initial state (after 1 warm-up)"}
+        out[wl] = rec
+    return out
 
 
 def aggregate_over_ranks(dist, local_ms: float, local_units: int):
@@ -413,6 +460,7 @@ def run_ours(args, workload):
     solver.close()
     batched = measure_batched(args) if (rank == 0 and not args.no_batched) else None
     adjoint = measure_adjoint(args) if (rank == 0 and not args.no_adjoint) else None
+    others = measure_other_workloads(args, workload) if (rank == 0 and not args.no_other_workloads) else None
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -442,6 +490,7 @@ def run_ours(args, workload):
         "cpu_baseline": cpu,
         "batched": batched,
         "adjoint": adjoint,
+        "other_workloads": others,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -459,6 +508,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=100)
     args = ap.parse_args()
     if args.warmup < 3:
