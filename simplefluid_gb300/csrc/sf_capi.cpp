@@ -289,7 +289,7 @@ sf_status sort_uploaded(sf_ctx* ctx, const float* pos3, const float* vel3) {
     sf::launch_load_aos(pos3, vel3, d.n, d.pos2, d.vel2, ctx->stream);
     sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
     sf::enqueue_sort_tail(d, ctx->stream);
-    if (ctx->frame) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
+    if (ctx->frame && ctx->c.adaptive) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
     SF_TRY(check_launch("initial sort"));
     ctx->sorted = true;
     return SF_OK;
@@ -1274,7 +1274,7 @@ SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_o
         sf::launch_load_sorted(d.io, d.io + 3 * (size_t)n, d.tmp, n, d.pos2, d.vel2, ctx->stream);
         sf::launch_hash_count(d, d.pos2, n, ctx->c, d.counts, d.key_slot, ctx->stream);
         sf::enqueue_sort_tail(d, ctx->stream);
-        sf::launch_init_maxima(d.vel, n, ctx->frame, ctx->stream);
+        if (ctx->c.adaptive) sf::launch_init_maxima(d.vel, n, ctx->frame, ctx->stream);
         SF_TRY(check_launch("load state"));
         SF_CUDA(cudaStreamSynchronize(ctx->stream));
         ctx->sorted = true;

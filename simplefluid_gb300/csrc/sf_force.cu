@@ -15,16 +15,17 @@
 namespace sf {
 namespace {
 
-template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kReach, bool kBatched>
-__global__ void __launch_bounds__(kBlockSize)
-    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
-            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-            uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
-            uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-            uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot,
-            float4* __restrict__ acc_out, float4* __restrict__ sums, FrameState* __restrict__ frame) {
-    const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
-    if (i >= n) return;
+// Forces on particle i, then (kIntegrate) its step and the next sort's
+// histogram entry, or (!kIntegrate) its acceleration.  With the adaptive
+// sub-step, v2 and a2 receive |v'|^2 and |a|^2 as float bits.
+template <bool kUseList, int kPrefetch, bool kIntegrate, int kReach, bool kBatched>
+__device__ __forceinline__ void force_one(
+    uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
+    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+    const SimConst& c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
+    float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint32_t* __restrict__ counts,
+    uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
+    float4* __restrict__ sums, const FrameState* __restrict__ frame, uint32_t& v2, uint32_t& a2) {
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 xi = pos[i];
     const float4 vi = vel[i];
@@ -98,14 +99,44 @@ __global__ void __launch_bounds__(kBlockSize)
     const uint32_t key = cell_key(c, x[0], x[1], x[2]);
     key_slot[i] = make_uint2(key, count_in_cell(key, counts, tile_sums));
     if (frame && c.adaptive) {
-        // maxima of |v'|^2 and |a|^2 (non-negative floats order like their bits)
-        const unsigned mask = __activemask();
-        const uint32_t v2 = __float_as_uint(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
-        const uint32_t a2 = __float_as_uint(fmaf(az, az, fmaf(ay, ay, ax * ax)));
-        const uint32_t mv = __reduce_max_sync(mask, v2), ma = __reduce_max_sync(mask, a2);
-        if ((threadIdx.x & 31) == (uint32_t)(__ffs(mask) - 1)) {
-            atomicMax(&frame->v2max_bits, mv);
-            atomicMax(&frame->a2max_bits, ma);
+        v2 = __float_as_uint(fmaf(v[2], v[2], fmaf(v[1], v[1], v[0] * v[0])));
+        a2 = __float_as_uint(fmaf(az, az, fmaf(ay, ay, ax * ax)));
+    }
+}
+
+template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kReach, bool kBatched>
+__global__ void __launch_bounds__(kBlockSize)
+    k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
+            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
+            uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
+            uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+            uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot,
+            float4* __restrict__ acc_out, float4* __restrict__ sums, FrameState* __restrict__ frame) {
+    const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
+    uint32_t v2 = 0u, a2 = 0u;
+    if (i < n)
+        force_one<kUseList, kPrefetch, kIntegrate, kReach, kBatched>(i, pos, vel, pr, cs, nbr, nbr_count, c0, table,
+                                                                     scene_off, nscenes, pos_out, vel_out, counts,
+                                                                     tile_sums, key_slot, acc_out, sums, frame, v2, a2);
+    if (!kBatched && kIntegrate && frame && c0.adaptive) {
+        // maxima of |v'|^2 and |a|^2 over the block (non-negative floats order
+        // like their bits), then one atomic each per block
+        __shared__ uint32_t s_max[2][kBlockSize / 32];
+        v2 = __reduce_max_sync(0xffffffffu, v2);
+        a2 = __reduce_max_sync(0xffffffffu, a2);
+        if ((threadIdx.x & 31) == 0) {
+            s_max[0][threadIdx.x / 32] = v2;
+            s_max[1][threadIdx.x / 32] = a2;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const bool have = threadIdx.x < kBlockSize / 32;
+            const uint32_t mv = __reduce_max_sync(0xffffffffu, have ? s_max[0][threadIdx.x] : 0u);
+            const uint32_t ma = __reduce_max_sync(0xffffffffu, have ? s_max[1][threadIdx.x] : 0u);
+            if (threadIdx.x == 0) {
+                atomicMax(&frame->v2max_bits, mv);
+                atomicMax(&frame->a2max_bits, ma);
+            }
         }
     }
 }

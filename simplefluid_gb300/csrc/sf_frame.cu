@@ -25,15 +25,26 @@ __global__ void k_choose_dt(FrameState* __restrict__ fs, SimConst c) {
     fs->a2max_bits = 0u;
 }
 
-__global__ void k_init_maxima(const float4* __restrict__ vel, uint32_t n, FrameState* __restrict__ fs) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// max |v|^2 of the state (non-negative floats order like their bits): one
+// atomic per block of kMaxBlock threads.
+constexpr uint32_t kMaxBlock = 1024;
+
+__global__ void __launch_bounds__(kMaxBlock)
+    k_init_maxima(const float4* __restrict__ vel, uint32_t n, FrameState* __restrict__ fs) {
+    __shared__ uint32_t s_max[kMaxBlock / 32];
+    const uint32_t i = blockIdx.x * kMaxBlock + threadIdx.x;
     uint32_t v2 = 0u;
     if (i < n) {
         const float4 v = vel[i];
         v2 = __float_as_uint(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
     }
-    const uint32_t m = __reduce_max_sync(0xffffffffu, v2);
-    if ((threadIdx.x & 31) == 0) atomicMax(&fs->v2max_bits, m);
+    v2 = __reduce_max_sync(0xffffffffu, v2);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x / 32] = v2;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const uint32_t m = __reduce_max_sync(0xffffffffu, s_max[threadIdx.x]);
+        if (threadIdx.x == 0) atomicMax(&fs->v2max_bits, m);
+    }
 }
 
 __global__ void k_frame_begin(FrameState* __restrict__ fs) {
@@ -59,7 +70,7 @@ void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s) { k_cho
 
 void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s) {
     cudaMemsetAsync(&fs->v2max_bits, 0, 2 * sizeof(uint32_t), s);
-    if (n) k_init_maxima<<<grid_for(n, kBlock), kBlock, 0, s>>>(vel, n, fs);
+    if (n) k_init_maxima<<<grid_for(n, kMaxBlock), kMaxBlock, 0, s>>>(vel, n, fs);
 }
 
 void launch_frame_begin(FrameState* fs, cudaStream_t s) { k_frame_begin<<<1, 32, 0, s>>>(fs); }
