@@ -59,6 +59,9 @@ struct sf_ctx {
     sf::DeviceState d{};
     int device = 0;
     cudaStream_t stream = nullptr;
+    // uploads: a second stream, so that the velocity copy overlaps the sort
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_pos = nullptr, ev_vel = nullptr;
     cudaGraphExec_t step_graph = nullptr;
     bool sorted = false;  // particles uploaded and cell-sorted
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
@@ -289,6 +292,34 @@ sf_status sort_uploaded(sf_ctx* ctx, const float* pos3, const float* vel3) {
     sf::launch_load_aos(pos3, vel3, d.n, d.pos2, d.vel2, ctx->stream);
     sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
     sf::enqueue_sort_tail(d, ctx->stream);
+    if (ctx->frame && ctx->c.adaptive) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
+    SF_TRY(check_launch("initial sort"));
+    ctx->sorted = true;
+    return SF_OK;
+}
+
+// Upload from page-locked host arrays: positions first, then the velocity
+// copy on the second stream while the positions are hashed, counted and
+// scattered; the gather waits for the velocities.
+sf_status upload_overlapped(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz) {
+    sf::DeviceState& d = ctx->d;
+    if (!ctx->aux) {
+        SF_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+        SF_CUDA(cudaEventCreateWithFlags(&ctx->ev_pos, cudaEventDisableTiming));
+        SF_CUDA(cudaEventCreateWithFlags(&ctx->ev_vel, cudaEventDisableTiming));
+    }
+    const size_t bytes = (size_t)d.n * 3 * sizeof(float);
+    float* io_pos = d.io;
+    float* io_vel = d.io + 3 * (size_t)d.n;
+    SF_CUDA(cudaMemcpyAsync(io_pos, pos_xyz, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    SF_CUDA(cudaEventRecord(ctx->ev_pos, ctx->stream));
+    SF_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->ev_pos, 0));  // after all earlier work on io
+    SF_CUDA(cudaMemcpyAsync(io_vel, vel_xyz, bytes, cudaMemcpyHostToDevice, ctx->aux));
+    sf::launch_load_vel(io_vel, d.n, d.vel2, ctx->aux);
+    SF_CUDA(cudaEventRecord(ctx->ev_vel, ctx->aux));
+    sf::launch_load_pos(io_pos, d.n, d.pos2, ctx->stream);
+    sf::launch_hash_count(d, d.pos2, d.n, ctx->c, d.counts, d.key_slot, ctx->stream);
+    sf::enqueue_sort_tail(d, ctx->stream, ctx->ev_vel);
     if (ctx->frame && ctx->c.adaptive) sf::launch_init_maxima(d.vel, d.n, ctx->frame, ctx->stream);
     SF_TRY(check_launch("initial sort"));
     ctx->sorted = true;
@@ -622,6 +653,12 @@ SF_API sf_status sf_destroy(sf_ctx* ctx) {
     free_particles(ctx->d);
     free_grid(ctx->d);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->aux) {
+        cudaStreamSynchronize(ctx->aux);
+        cudaStreamDestroy(ctx->aux);
+    }
+    if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
+    if (ctx->ev_vel) cudaEventDestroy(ctx->ev_vel);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SF_OK;
@@ -679,6 +716,11 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
     ctx->d.n = n;
     ctx->sorted = false;
     if (n == 0) return SF_OK;
+    if (vel_xyz && is_pinned(pos_xyz) && is_pinned(vel_xyz)) {
+        SF_TRY(upload_overlapped(ctx, pos_xyz, vel_xyz));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
     float* io = ctx->d.io;
     const size_t bytes = (size_t)n * 3 * sizeof(float);
     SF_TRY(copy_in(ctx, io, pos_xyz, bytes));

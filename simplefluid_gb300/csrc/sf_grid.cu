@@ -25,6 +25,19 @@ __global__ void k_load_aos(const float* __restrict__ pos3, const float* __restri
         vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// The two halves of k_load_aos, for uploads whose velocities arrive later.
+__global__ void k_load_pos(const float* __restrict__ pos3, uint32_t n, float4* __restrict__ pos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pos[i] = make_float4(pos3[3 * (size_t)i], pos3[3 * (size_t)i + 1], pos3[3 * (size_t)i + 2], __uint_as_float(i));
+}
+
+__global__ void k_load_vel(const float* __restrict__ vel3, uint32_t n, float4* __restrict__ vel) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vel[i] = make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.f);
+}
+
 // Sorted state with explicit particle indices (state files).
 __global__ void k_load_sorted(const float* __restrict__ pos3, const float* __restrict__ vel3,
                               const uint32_t* __restrict__ ids, uint32_t n, float4* __restrict__ pos,
@@ -208,6 +221,14 @@ void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* p
     if (n) k_load_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, n, pos, vel);
 }
 
+void launch_load_pos(const float* pos3, uint32_t n, float4* pos, cudaStream_t s) {
+    if (n) k_load_pos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, n, pos);
+}
+
+void launch_load_vel(const float* vel3, uint32_t n, float4* vel, cudaStream_t s) {
+    if (n) k_load_vel<<<grid_for(n, kBlock), kBlock, 0, s>>>(vel3, n, vel);
+}
+
 void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* ids, uint32_t n, float4* pos,
                         float4* vel, cudaStream_t s) {
     if (n) k_load_sorted<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, ids, n, pos, vel);
@@ -278,9 +299,10 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
     });
 }
 
-void enqueue_sort_tail(DeviceState& d, cudaStream_t s) {
+void enqueue_sort_tail(DeviceState& d, cudaStream_t s, cudaEvent_t before_gather) {
     launch_scan_cells(d, d.n, s);
     launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, d.ntiles, s);
+    if (before_gather) cudaStreamWaitEvent(s, before_gather, 0);
     launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
 }
 

@@ -112,6 +112,8 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 
 // ---- kernel launchers (sf_grid.cu, sf_density.cu, sf_force.cu); all enqueue on `s`
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
+void launch_load_pos(const float* pos3, uint32_t n, float4* pos, cudaStream_t s);
+void launch_load_vel(const float* vel3, uint32_t n, float4* vel, cudaStream_t s);
 void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* ids, uint32_t n, float4* pos,
                         float4* vel, cudaStream_t s);
 void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, uint32_t* ids,
@@ -137,7 +139,7 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
 
 // The sort tail shared by makeReady and every step: counts -> cell_start,
 // bucket (clearing the counters), stable rank, gather pos2/vel2 -> pos/vel.
-void enqueue_sort_tail(DeviceState& d, cudaStream_t s);
+void enqueue_sort_tail(DeviceState& d, cudaStream_t s, cudaEvent_t before_gather = nullptr);
 // One full sub-step on the sorted state.
 void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s);
 
