@@ -132,10 +132,16 @@ SF_API sf_status sf_set_params(sf_ctx* ctx, const sf_params* p);
 SF_API sf_status sf_get_params(const sf_ctx* ctx, sf_params* p);
 
 /* ---- particle state: getParticles() / getVelocity() --------------------- */
-/* Copy a host AoS float3 state in.  vel_xyz may be NULL (zero velocity). */
+/* Copy a host AoS float3 state in (n * 3 floats each).  vel_xyz may be NULL
+ * (zero velocity).  Page-locked arrays (sf_host_alloc) are copied by DMA, the
+ * velocities while the positions are sorted.  Pageable arrays are read by the
+ * GPU in place where it accesses pageable memory through the host's page
+ * tables (Grace: NVLink-C2C), else staged through a page-locked buffer. */
 SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz, uint32_t n);
 /* Copy the state out in the caller's original particle order.  Either output
- * may be NULL.  Waits for the context's stream. */
+ * may be NULL.  Page-locked arrays are filled by DMA; pageable ones are
+ * written by the GPU in place where it can, else through staging.  Waits for
+ * the context's stream. */
 SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint32_t n);
 /* getNumParticles() */
 SF_API sf_status sf_get_num_particles(const sf_ctx* ctx, uint32_t* n_out);

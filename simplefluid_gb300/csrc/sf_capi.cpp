@@ -62,6 +62,9 @@ struct sf_ctx {
     // uploads: a second stream, so that the velocity copy overlaps the sort
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_pos = nullptr, ev_vel = nullptr;
+    // the GPU reads and writes pageable host memory through the host's page
+    // tables (Grace: NVLink-C2C with address translation): -1 unknown, 0, 1
+    int host_direct = -1;
     cudaGraphExec_t step_graph = nullptr;
     bool sorted = false;  // particles uploaded and cell-sorted
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
@@ -150,6 +153,28 @@ sf_status ensure_stage(sf_ctx* ctx, size_t bytes) {
     SF_CUDA(cudaMallocHost(&ctx->h_stage, bytes));
     ctx->h_stage_bytes = bytes;
     return SF_OK;
+}
+
+// Pageable (not page-locked, not device) host memory that the context's GPU
+// can read and write in place: the device accesses pageable memory through
+// the host's page tables.
+bool host_direct(sf_ctx* ctx, const void* p) {
+    if (ctx->host_direct < 0) {
+        int a = 0, b = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, ctx->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) != cudaSuccess) {
+            cudaGetLastError();
+            a = b = 0;
+        }
+        ctx->host_direct = (a && b) ? 1 : 0;
+    }
+    if (!ctx->host_direct) return false;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeUnregistered;
 }
 
 bool is_pinned(const void* p) {
@@ -721,6 +746,12 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
         SF_CUDA(cudaStreamSynchronize(ctx->stream));
         return SF_OK;
     }
+    if (host_direct(ctx, pos_xyz) && (!vel_xyz || host_direct(ctx, vel_xyz))) {
+        // pageable arrays the GPU reads in place: no staging copy
+        SF_TRY(sort_uploaded(ctx, pos_xyz, vel_xyz));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
     float* io = ctx->d.io;
     const size_t bytes = (size_t)n * 3 * sizeof(float);
     SF_TRY(copy_in(ctx, io, pos_xyz, bytes));
@@ -735,6 +766,13 @@ SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint3
     SF_TRY(need_sorted(ctx));
     if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
     SF_TRY(set_device(ctx));
+    if ((pos_xyz || vel_xyz) && (!pos_xyz || host_direct(ctx, pos_xyz)) && (!vel_xyz || host_direct(ctx, vel_xyz))) {
+        // pageable arrays the GPU writes in place: no staging copy
+        sf::launch_store_caller_order(ctx->d.pos, ctx->d.vel, n, ctx->d.tmp, pos_xyz, vel_xyz, ctx->stream);
+        SF_TRY(check_launch("store state"));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
     float* io = ctx->d.io;
     const size_t bytes = (size_t)n * 3 * sizeof(float);
     sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, pos_xyz ? io : nullptr, vel_xyz ? io + 3 * (size_t)n : nullptr,

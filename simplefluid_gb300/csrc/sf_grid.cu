@@ -83,6 +83,38 @@ __global__ void k_store_aos(const float4* __restrict__ pos, const float4* __rest
     }
 }
 
+// Sorted slot of every caller index.
+__global__ void k_slot_of_caller(const float4* __restrict__ pos, uint32_t n, uint32_t* __restrict__ slot) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = __float_as_uint(pos[i].w);
+    if (id < n) slot[id] = i;
+}
+
+// Caller-order AoS state gathered through the slot map: consecutive threads
+// write consecutive particles, so the stores stay coalesced when the arrays
+// are host memory that the kernel writes over the CPU-GPU link.
+__global__ void k_store_caller_order(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                     const uint32_t* __restrict__ slot, uint32_t n, float* __restrict__ pos3,
+                                     float* __restrict__ vel3) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t i = slot[t];
+    if (i >= n) return;  // never for a consistent state
+    if (pos3) {
+        const float4 p = pos[i];
+        pos3[3 * (size_t)t] = p.x;
+        pos3[3 * (size_t)t + 1] = p.y;
+        pos3[3 * (size_t)t + 2] = p.z;
+    }
+    if (vel3) {
+        const float4 v = vel[i];
+        vel3[3 * (size_t)t] = v.x;
+        vel3[3 * (size_t)t + 1] = v.y;
+        vel3[3 * (size_t)t + 2] = v.z;
+    }
+}
+
 // ---------------------------------------------------------------- hashing
 // Histogram of an uploaded (not cell-sorted) state.  Its lanes hit scattered
 // scan tiles, so the tile totals come from a separate reduction instead of
@@ -241,6 +273,13 @@ void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float
 
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s) {
     if (n) k_store_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, vel, n, pos3, vel3);
+}
+
+void launch_store_caller_order(const float4* pos, const float4* vel, uint32_t n, uint32_t* slot, float* pos3,
+                               float* vel3, cudaStream_t s) {
+    if (!n) return;
+    k_slot_of_caller<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, n, slot);
+    k_store_caller_order<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos, vel, slot, n, pos3, vel3);
 }
 
 void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,

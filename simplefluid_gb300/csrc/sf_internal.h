@@ -119,6 +119,10 @@ void launch_load_sorted(const float* pos3, const float* vel3, const uint32_t* id
 void launch_store_sorted(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, uint32_t* ids,
                          cudaStream_t s);
 void launch_store_aos(const float4* pos, const float4* vel, uint32_t n, float* pos3, float* vel3, cudaStream_t s);
+// Caller-order AoS output with coalesced stores (for host memory that the
+// kernel writes directly); `slot` is n entries of scratch.
+void launch_store_caller_order(const float4* pos, const float4* vel, uint32_t n, uint32_t* slot, float* pos3,
+                               float* vel3, cudaStream_t s);
 // Cell keys and histogram of an uploaded state, and its scan-tile totals.
 void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* counts,
                        uint2* key_slot, cudaStream_t s);
