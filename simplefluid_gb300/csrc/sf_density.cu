@@ -25,6 +25,8 @@ __global__ void __launch_bounds__(kBlockSize)
               float* __restrict__ rho_out, float2* __restrict__ pr_out, uint32_t* __restrict__ nbr,
               uint32_t* __restrict__ nbr_count) {
     __shared__ uint32_t s_nb[kMode == kEmitStaged ? kNbCap : 1][kMode == kEmitStaged ? kBlockSize : 1];
+    grid_dependency_wait();
+    allow_dependents();
     const uint32_t t = threadIdx.x;
     const uint32_t i = blockIdx.x * kBlockSize + t;
     uint32_t cnt = 0;
@@ -65,11 +67,12 @@ void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
         constexpr int K = decltype(R)::value;
         if (d.table) {
             if constexpr (K <= 2)
-                k_density<kMode, kBlockSize, K, true><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-                    d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, d.rho, d.pr, d.nbr, d.nbr_count);
+                launch_chained(k_density<kMode, kBlockSize, K, true>, grid_for(d.n, kBlockSize), kBlockSize, s,
+                               d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, d.rho, d.pr, d.nbr,
+                               d.nbr_count);
         } else {
-            k_density<kMode, kBlockSize, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-                d.pos, d.cell_start, d.n, c, nullptr, nullptr, 0, d.rho, d.pr, d.nbr, d.nbr_count);
+            launch_chained(k_density<kMode, kBlockSize, K, false>, grid_for(d.n, kBlockSize), kBlockSize, s, d.pos,
+                           d.cell_start, d.n, c, nullptr, nullptr, 0u, d.rho, d.pr, d.nbr, d.nbr_count);
         }
     });
 }

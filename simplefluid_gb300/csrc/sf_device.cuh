@@ -16,6 +16,30 @@ constexpr int kBlock = 256;
 
 inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Programmatic dependent launch.  The kernels of a sub-step are launched with
+// launch_chained(): each may begin launching while its predecessor in the
+// stream finishes.  Every such kernel calls grid_dependency_wait() before it
+// touches global memory (it returns once the predecessor has completed and its
+// writes are visible; a no-op without one), then allow_dependents() so that
+// the next kernel's blocks are scheduled during this kernel's last wave.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_chained(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Calls f(std::integral_constant<int, K>) for the context's reach K.
 template <typename F>
 inline void with_reach(int reach, F&& f) {

@@ -112,6 +112,8 @@ __global__ void __launch_bounds__(kBlockSize)
             uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot,
             float4* __restrict__ acc_out, float4* __restrict__ sums, FrameState* __restrict__ frame) {
+    grid_dependency_wait();
+    allow_dependents();
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     uint32_t v2 = 0u, a2 = 0u;
     if (i < n)
@@ -153,14 +155,14 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
         float4* ac = kIntegrate ? nullptr : d.accel;
         if (d.table) {
             if constexpr (K <= 2 && kPrefetch == 2)
-                k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>
-                    <<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(d.pos, d.vel, d.pr, d.cell_start, d.nbr,
-                                                                     d.nbr_count, d.n, c, d.table, d.scene_off,
-                                                                     d.nscenes, po, vo, co, ts, ks, ac, d.sums, nullptr);
+                launch_chained(k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>, grid_for(d.n, kBlockSize),
+                               kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, d.table,
+                               d.scene_off, d.nscenes, po, vo, co, ts, ks, ac, d.sums, (FrameState*)nullptr);
         } else {
-            k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false><<<grid_for(d.n, kBlockSize), kBlockSize, 0, s>>>(
-                d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, nullptr, nullptr, 0, po, vo, co, ts, ks,
-                ac, d.sums, kIntegrate ? d.frame : nullptr);
+            launch_chained(k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false>, grid_for(d.n, kBlockSize),
+                           kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c,
+                           (const SimConst*)nullptr, (const uint32_t*)nullptr, 0u, po, vo, co, ts, ks, ac, d.sums,
+                           kIntegrate ? d.frame : nullptr);
         }
     });
 }

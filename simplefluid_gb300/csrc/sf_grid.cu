@@ -186,6 +186,8 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_totals(const uint4* __res
 __global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__ counts,
                                                        const uint32_t* __restrict__ tile_sums,
                                                        uint4* __restrict__ cell_start) {
+    grid_dependency_wait();
+    allow_dependents();
     __shared__ uint32_t total;
     uint32_t before = 0;
     for (uint32_t t = threadIdx.x; t < blockIdx.x; t += kScanThreads) before += tile_sums[t];
@@ -202,6 +204,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__
 // next step (only those were counted, so this leaves every counter zero).
 __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start, uint32_t n,
                           uint32_t* __restrict__ tmp, uint32_t* __restrict__ counts) {
+    grid_dependency_wait();
+    allow_dependents();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 ks = key_slot[i];
@@ -212,8 +216,12 @@ __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __
 __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t* __restrict__ cell_start,
                               const uint32_t* __restrict__ tmp, const float4* __restrict__ pos_in,
                               const float4* __restrict__ vel_in, uint32_t n, float4* __restrict__ pos_out,
-                              float4* __restrict__ vel_out) {
+                              float4* __restrict__ vel_out, uint32_t* __restrict__ tile_sums, uint32_t ntiles) {
+    grid_dependency_wait();
+    allow_dependents();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the scan-tile totals are zero again for the next histogram
+    for (uint32_t t = i; t < ntiles; t += gridDim.x * blockDim.x) tile_sums[t] = 0u;
     if (i >= n) return;
     const uint32_t key = key_slot[i].x;
     const uint32_t b = cell_start[key], e = cell_start[key + 1];
@@ -303,23 +311,24 @@ void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimC
 }
 
 void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
-    k_scan<<<d.ntiles, kScanThreads, 0, s>>>(reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
-                                             reinterpret_cast<uint4*>(d.cell_start));
+    launch_chained(k_scan, d.ntiles, kScanThreads, s, reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
+                   reinterpret_cast<uint4*>(d.cell_start));
 }
 
-// Buckets indices by cell and clears the counters; the scan-tile totals (a
-// few KB) are cleared with one memset.
+// Buckets indices by cell and clears the counters.
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    uint32_t* tile_sums, uint32_t ntiles, cudaStream_t s) {
-    if (n) k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, n, tmp, counts);
-    cudaMemsetAsync(tile_sums, 0, (size_t)ntiles * sizeof(uint32_t), s);
+                    cudaStream_t s) {
+    if (n) launch_chained(k_scatter, grid_for(n, kBlock), kBlock, s, key_slot, cell_start, n, tmp, counts);
 }
 
+// Stable rank inside each cell and the gather; also zeroes the scan-tile
+// totals (ntiles entries) for the next histogram.
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
-                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s) {
+                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, uint32_t* tile_sums,
+                        uint32_t ntiles, cudaStream_t s) {
     if (n)
-        k_rank_gather<<<grid_for(n, kBlock), kBlock, 0, s>>>(key_slot, cell_start, tmp, pos_in, vel_in, n, pos_out,
-                                                             vel_out);
+        launch_chained(k_rank_gather, grid_for(n, kBlock), kBlock, s, key_slot, cell_start, tmp, pos_in, vel_in, n,
+                       pos_out, vel_out, tile_sums, ntiles);
 }
 
 void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
@@ -340,9 +349,9 @@ void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* c
 
 void enqueue_sort_tail(DeviceState& d, cudaStream_t s, cudaEvent_t before_gather) {
     launch_scan_cells(d, d.n, s);
-    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, d.ntiles, s);
+    launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s);
     if (before_gather) cudaStreamWaitEvent(s, before_gather, 0);
-    launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s);
+    launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, d.tile_sums, d.ntiles, s);
 }
 
 const char* const kStageNames[kNumStages] = {"density", "force_integrate", "scan", "scatter", "rank_gather"};
@@ -352,8 +361,11 @@ void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream
         case 0: launch_density(d, c, s); break;
         case 1: launch_force_integrate(d, c, s); break;
         case 2: launch_scan_cells(d, d.n, s); break;
-        case 3: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, d.tile_sums, d.ntiles, s); break;
-        case 4: launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, s); break;
+        case 3: launch_scatter(d.key_slot, d.cell_start, d.n, d.tmp, d.counts, s); break;
+        case 4:
+            launch_rank_gather(d.key_slot, d.cell_start, d.tmp, d.pos2, d.vel2, d.n, d.pos, d.vel, d.tile_sums,
+                               d.ntiles, s);
+            break;
         default: break;
     }
 }

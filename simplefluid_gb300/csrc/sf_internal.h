@@ -128,9 +128,11 @@ void launch_hash_count(const DeviceState& d, const float4* pos, uint32_t n, cons
                        uint2* key_slot, cudaStream_t s);
 void launch_scan_cells(DeviceState& d, uint32_t n, cudaStream_t s);
 void launch_scatter(const uint2* key_slot, const uint32_t* cell_start, uint32_t n, uint32_t* tmp, uint32_t* counts,
-                    uint32_t* tile_sums, uint32_t ntiles, cudaStream_t s);
+                    cudaStream_t s);
+// also zeroes tile_sums (ntiles entries) for the next histogram
 void launch_rank_gather(const uint2* key_slot, const uint32_t* cell_start, const uint32_t* tmp, const float4* pos_in,
-                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, cudaStream_t s);
+                        const float4* vel_in, uint32_t n, float4* pos_out, float4* vel_out, uint32_t* tile_sums,
+                        uint32_t ntiles, cudaStream_t s);
 void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
 // forces + symplectic Euler + box + next-step cell hash into pos2/vel2
 void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s);
