@@ -186,8 +186,14 @@ template <int kReach, typename F>
 __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
                                                const float4* __restrict__ pos, float x, float y, float z, F&& f) {
     for_candidate_rows<kReach>(c, cs, x, y, z, [&](uint32_t b, uint32_t e) {
+        uint32_t j = b;
 #pragma unroll 1
-        for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+        for (; j + 1 < e; j += 2) {
+            const float4 x0 = ldg4(pos + j), x1 = ldg4(pos + j + 1);
+            f(j, x0);
+            f(j + 1, x1);
+        }
+        if (j < e) f(j, ldg4(pos + j));
     });
 }
 
