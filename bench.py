@@ -420,11 +420,14 @@ def run_ours(args, workload):
         bytes_per_launch = STAGE_BYTES_PER_CELL.get(dom, 0) * ncells
     peaks = measured_peaks()
     achieved = bytes_per_launch / (avg_ms[dom] * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    # DRAM traffic and issue figures of one ncu capture of the same kernel
+    # (profiles/ncu_figures.json; per launch, step 7 of this workload)
+    traffic, ncu_fig = None, {}
+    tpath = os.path.join(ROOT, "profiles", "ncu_figures.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(workload, {}).get(dom)
+            ncu_fig = json.load(f).get(workload, {}).get(dom, {})
+        traffic = ncu_fig.get("traffic_bytes")
 
     # e2e through the C ABI with pinned host buffers
     nbytes = n * 3 * 4
@@ -484,7 +487,12 @@ def run_ours(args, workload):
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": peaks["source"], "algorithmic_bytes_per_launch": bytes_per_launch,
                      "avg_launch_ms": avg_ms[dom],
-                     "step_frac": STEP_BYTES_PER_UPDATE * value / 1e9 / peaks["hbm_gbs"]},
+                     "step_frac": STEP_BYTES_PER_UPDATE * value / 1e9 / peaks["hbm_gbs"],
+                     "ncu": {k: ncu_fig[k] for k in ("issue_active_pct", "ipc", "warps_active_pct",
+                                                     "long_scoreboard_per_issue") if k in ncu_fig},
+                     "note": ("bound by instruction issue, not HBM (ncu issue-active above)"
+                              if ncu_fig.get("issue_active_pct", 0) >= 70 else
+                              "bound by the latency of dependent loads, not HBM bandwidth (ncu above)")},
         "stages_ms": avg_ms,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
                 "path": "sf_set_state(pinned host) + sf_advance_frame + sf_get_state(pinned host)",
