@@ -228,6 +228,23 @@ SF_API sf_status sf_compute_accel(sf_ctx* ctx, float* accel_xyz, uint32_t n);
  * order-independent hash of their original indices. */
 SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash, uint32_t n);
 
+/* ---- failure detection: invariants of the current state -------------------
+ * Counted on the GPU over the cell-sorted state; a healthy state has every
+ * count zero except possibly list_overflow.  Waits for the stream. */
+typedef struct sf_state_report {
+    uint32_t n;                   /* particles                                       */
+    uint32_t non_finite;          /* NaN or Inf in a position or velocity            */
+    uint32_t outside_box;         /* outside [box_min + r, box_max - r] (only before
+                                     the first step after an upload)                 */
+    uint32_t unsorted;            /* sorted neighbours whose cell keys decrease      */
+    uint32_t cell_table_mismatch; /* particles outside their cell's table range      */
+    uint32_t bad_ids;             /* caller indices out of range, repeated or absent */
+    uint32_t list_overflow;       /* neighbour lists of the last density pass that
+                                     exceeded their capacity (rescanned, correct)    */
+    float max_speed;              /* max |v| over finite particles                   */
+} sf_state_report;
+SF_API sf_status sf_check_state(sf_ctx* ctx, sf_state_report* report);
+
 /* ---- kernel tuning -----------------------------------------------------------
  * Implementation choices of a context's step.  Every choice computes the same
  * bits; they differ only in speed.  Not part of the reference interface. */
@@ -353,6 +370,8 @@ SF_API sf_status sf_batch_get_state(sf_batch* b, float* pos_xyz, float* vel_xyz,
 SF_API sf_status sf_batch_num_particles(const sf_batch* b, uint32_t* n_out);
 /* `nsteps` sub-steps of every scene: one graph launch per step. */
 SF_API sf_status sf_batch_step(sf_batch* b, uint32_t nsteps);
+/* sf_check_state over all scenes of the batch. */
+SF_API sf_status sf_batch_check_state(sf_batch* b, sf_state_report* report);
 SF_API sf_status sf_batch_synchronize(sf_batch* b);
 SF_API sf_status sf_batch_step_timed(sf_batch* b, uint32_t nsteps, uint64_t flush_bytes, float* total_ms,
                                      float* step_ms);

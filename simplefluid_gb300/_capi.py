@@ -104,6 +104,17 @@ class sf_device_view(ctypes.Structure):
                 ("cell_start", c_void_p), ("n", c_uint32), ("ncells", c_uint32), ("stream", c_void_p)]
 
 
+class sf_state_report(ctypes.Structure):
+    """Mirror of ``struct sf_state_report`` (include/sf_capi.h)."""
+
+    _fields_ = [("n", c_uint32), ("non_finite", c_uint32), ("outside_box", c_uint32), ("unsorted", c_uint32),
+                ("cell_table_mismatch", c_uint32), ("bad_ids", c_uint32), ("list_overflow", c_uint32),
+                ("max_speed", c_float)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class SFError(RuntimeError):
     """Raised when a C-ABI call returns a non-zero sf_status."""
 
@@ -131,6 +142,8 @@ PROTOTYPES = {
     "sf_set_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
     "sf_get_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
     "sf_device_state": (c_int32, [c_void_p, _P(sf_device_view)]),
+    "sf_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
+    "sf_batch_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
     "sf_get_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
     "sf_make_ready": (c_int32, [c_void_p]),
     "sf_advance_frame": (c_int32, [c_void_p, _P(c_float)]),

@@ -65,6 +65,7 @@ struct sf_ctx {
     // the GPU reads and writes pageable host memory through the host's page
     // tables (Grace: NVLink-C2C with address translation): -1 unknown, 0, 1
     int host_direct = -1;
+    uint32_t* d_report = nullptr;  // sf_check_state counters
     cudaGraphExec_t step_graph = nullptr;
     bool sorted = false;  // particles uploaded and cell-sorted
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
@@ -294,6 +295,7 @@ sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     const size_t tiles = (c + sf::kNbTile - 1) / sf::kNbTile;
     SF_CUDA(cudaMalloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t)));
     SF_CUDA(cudaMalloc(&d.nbr_count, c * sizeof(uint32_t)));
+    SF_CUDA(cudaMemset(d.nbr_count, 0, c * sizeof(uint32_t)));
     d.cap = (uint32_t)c;
     return SF_OK;
 }
@@ -666,25 +668,40 @@ SF_API sf_status sf_create(const sf_params* p, sf_ctx** out) {
     return SF_OK;
 }
 
-SF_API sf_status sf_destroy(sf_ctx* ctx) {
-    if (!ctx) return SF_OK;
+namespace {
+
+// Every resource a context owns (also the engine embedded in a batch).
+void release_ctx(sf_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->aux) cudaStreamSynchronize(ctx->aux);
     free_trajectory(ctx);
     free_render(ctx);
     if (ctx->frame_graph) cudaGraphExecDestroy(ctx->frame_graph);
+    ctx->frame_graph = nullptr;
     if (ctx->frame) cudaFree(ctx->frame);
+    ctx->frame = nullptr;
     drop_graph(ctx);
     free_particles(ctx->d);
     free_grid(ctx->d);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-    if (ctx->aux) {
-        cudaStreamSynchronize(ctx->aux);
-        cudaStreamDestroy(ctx->aux);
-    }
+    ctx->h_stage = nullptr;
+    if (ctx->d_report) cudaFree(ctx->d_report);
+    ctx->d_report = nullptr;
     if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
     if (ctx->ev_vel) cudaEventDestroy(ctx->ev_vel);
+    ctx->ev_pos = ctx->ev_vel = nullptr;
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    ctx->aux = nullptr;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    ctx->stream = nullptr;
+}
+
+}  // namespace
+
+SF_API sf_status sf_destroy(sf_ctx* ctx) {
+    if (!ctx) return SF_OK;
+    release_ctx(ctx);
     delete ctx;
     return SF_OK;
 }
@@ -1064,6 +1081,32 @@ SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash
     SF_TRY(check_launch("neighbour stats"));
     SF_TRY(copy_out(ctx, count, dc, (size_t)n * sizeof(uint32_t)));
     SF_TRY(copy_out(ctx, hash, dh, (size_t)n * sizeof(uint32_t)));
+    return SF_OK;
+}
+
+SF_API sf_status sf_check_state(sf_ctx* ctx, sf_state_report* report) {
+    SF_TRY(need_sorted(ctx));
+    if (!report) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
+    SF_TRY(set_device(ctx));
+    if (!ctx->d_report) SF_CUDA(cudaMalloc(&ctx->d_report, sf::kReportWords * sizeof(uint32_t)));
+    // the bucketed-index buffer is free between steps: it holds the id tally
+    const bool lists = ctx->d.nbr && ctx->d.tune.list_mode != SF_LIST_NONE;
+    sf::launch_check_state(ctx->d, ctx->c, lists ? ctx->d.nbr_count : nullptr, ctx->d.tmp, ctx->d_report,
+                           ctx->stream);
+    SF_TRY(check_launch("check state"));
+    uint32_t r[sf::kReportWords];
+    SF_CUDA(cudaMemcpyAsync(r, ctx->d_report, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    report->n = ctx->d.n;
+    report->non_finite = r[0];
+    report->outside_box = r[1];
+    report->unsorted = r[2];
+    report->cell_table_mismatch = r[3];
+    report->bad_ids = r[4];
+    report->list_overflow = r[5];
+    float v2;
+    std::memcpy(&v2, &r[6], sizeof(v2));
+    report->max_speed = std::sqrt(v2);
     return SF_OK;
 }
 
@@ -1490,17 +1533,9 @@ SF_API sf_status sf_batch_create(const sf_params* per_scene, uint32_t nscenes, s
 
 SF_API sf_status sf_batch_destroy(sf_batch* b) {
     if (!b) return SF_OK;
-    cudaSetDevice(b->eng.device);
-    if (b->eng.stream) cudaStreamSynchronize(b->eng.stream);
-    drop_graph(&b->eng);
-    free_particles(b->eng.d);
-    free_grid(b->eng.d);
-    if (b->eng.h_stage) cudaFreeHost(b->eng.h_stage);
+    release_ctx(&b->eng);
     if (b->d_table) cudaFree(b->d_table);
     if (b->d_off) cudaFree(b->d_off);
-    if (b->eng.stream) cudaStreamDestroy(b->eng.stream);
-    b->eng.stream = nullptr;
-    b->eng.h_stage = nullptr;
     delete b;
     return SF_OK;
 }
@@ -1549,6 +1584,11 @@ SF_API sf_status sf_batch_num_particles(const sf_batch* b, uint32_t* n_out) {
 SF_API sf_status sf_batch_step(sf_batch* b, uint32_t nsteps) {
     SF_TRY(need_batch(b));
     return sf_step(&b->eng, nsteps);
+}
+
+SF_API sf_status sf_batch_check_state(sf_batch* b, sf_state_report* report) {
+    SF_TRY(need_batch(b));
+    return sf_check_state(&b->eng, report);
 }
 
 SF_API sf_status sf_batch_synchronize(sf_batch* b) {

@@ -254,9 +254,69 @@ __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t
     hash[i] = h;
 }
 
+// Invariants of a cell-sorted state, counted into r[]: 0 non-finite
+// particles, 1 particles outside the clamp box, 2 sorted neighbours whose cell
+// keys decrease, 3 particles outside their cell's table range, 4 caller
+// indices out of range (the rest are counted in `seen`), 5 neighbour lists
+// that overflowed in the last density pass, 6 max |v|^2 (float bits).
+template <bool kBatched>
+__global__ void __launch_bounds__(kBlock)
+    k_check_state(const float4* __restrict__ pos, const float4* __restrict__ vel, const uint32_t* __restrict__ cs,
+                  const uint32_t* __restrict__ nbr_count, uint32_t n, SimConst c0,
+                  const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
+                  uint32_t* __restrict__ seen, uint32_t* __restrict__ r) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t v2 = 0u;
+    if (i < n) {
+        const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
+        const float4 p = pos[i], v = vel[i];
+        const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) &&
+                            isfinite(v.z);
+        if (!finite) atomicAdd(r + 0, 1u);
+        if (finite && (p.x < c.lo[0] || p.x > c.hi[0] || p.y < c.lo[1] || p.y > c.hi[1] || p.z < c.lo[2] ||
+                       p.z > c.hi[2]))
+            atomicAdd(r + 1, 1u);
+        const uint32_t key = cell_key(c, p.x, p.y, p.z);
+        if (i > 0) {
+            const SimConst cq = const_of<kBatched>(c0, table, scene_off, nscenes, i - 1);
+            const float4 q = pos[i - 1];
+            if (cell_key(cq, q.x, q.y, q.z) > key) atomicAdd(r + 2, 1u);
+        }
+        if (!(cs[key] <= i && i < cs[key + 1])) atomicAdd(r + 3, 1u);
+        const uint32_t id = __float_as_uint(p.w);
+        if (id < n)
+            atomicAdd(seen + id, 1u);
+        else
+            atomicAdd(r + 4, 1u);
+        if (nbr_count && nbr_count[i] > (uint32_t)kNbCap) atomicAdd(r + 5, 1u);
+        if (finite) v2 = __float_as_uint(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
+    }
+    v2 = __reduce_max_sync(0xffffffffu, v2);
+    if ((threadIdx.x & 31) == 0 && v2) atomicMax(r + 6, v2);
+}
+
+// Caller indices not seen exactly once.
+__global__ void k_check_ids(const uint32_t* __restrict__ seen, uint32_t n, uint32_t* __restrict__ r) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && seen[i] != 1u) atomicAdd(r + 4, 1u);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
+void launch_check_state(const DeviceState& d, const SimConst& c, const uint32_t* nbr_count, uint32_t* seen,
+                        uint32_t* report, cudaStream_t s) {
+    cudaMemsetAsync(report, 0, kReportWords * sizeof(uint32_t), s);
+    if (!d.n) return;
+    cudaMemsetAsync(seen, 0, (size_t)d.n * sizeof(uint32_t), s);
+    if (d.table)
+        k_check_state<true><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.cell_start, nbr_count, d.n, c,
+                                                                     d.table, d.scene_off, d.nscenes, seen, report);
+    else
+        k_check_state<false><<<grid_for(d.n, kBlock), kBlock, 0, s>>>(d.pos, d.vel, d.cell_start, nbr_count, d.n, c,
+                                                                      nullptr, nullptr, 0, seen, report);
+    k_check_ids<<<grid_for(d.n, kBlock), kBlock, 0, s>>>(seen, d.n, report);
+}
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s) {
     if (n) k_load_aos<<<grid_for(n, kBlock), kBlock, 0, s>>>(pos3, vel3, n, pos, vel);
 }

@@ -140,6 +140,11 @@ void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s);
 void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s);
 void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
                  cudaStream_t s);
+// State invariants for sf_check_state: `seen` is n words of scratch, `report`
+// kReportWords words (see k_check_state).
+constexpr uint32_t kReportWords = 8;
+void launch_check_state(const DeviceState& d, const SimConst& c, const uint32_t* nbr_count, uint32_t* seen,
+                        uint32_t* report, cudaStream_t s);
 void launch_neighbour_stats(const DeviceState& d, const SimConst& c, uint32_t* count, uint32_t* hash,
                             cudaStream_t s);
 

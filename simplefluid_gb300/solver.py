@@ -225,6 +225,14 @@ class SPHSolver:
             ptrs.append(ptr)
         C.check(self._lib.sf_get_state_device(self._ctx, ptrs[0], ptrs[1], n, _stream_handle(stream, particles)))
 
+    def checkState(self) -> dict:
+        """Invariants of the current state counted on the GPU (sf_check_state):
+        non-finite values, particles outside the box, sort and cell-table
+        consistency, caller-index permutation, list overflows, max speed."""
+        r = C.sf_state_report()
+        C.check(self._lib.sf_check_state(self._ctx, byref(r)))
+        return r.as_dict()
+
     def deviceState(self) -> "C.sf_device_view":
         """Device pointers to the cell-sorted working arrays (sf_device_view)."""
         v = C.sf_device_view()
@@ -616,6 +624,12 @@ class SPHBatch:
         vel = np.empty((n, 3), np.float32)
         C.check(self._lib.sf_batch_get_state(self._b, _vp(pos), _vp(vel), n))
         return pos, vel
+
+    def checkState(self) -> dict:
+        """sf_check_state over all scenes (see SPHSolver.checkState)."""
+        r = C.sf_state_report()
+        C.check(self._lib.sf_batch_check_state(self._b, byref(r)))
+        return r.as_dict()
 
     def getParams(self, scene: int) -> C.sf_params:
         p = C.sf_params()
