@@ -245,6 +245,13 @@ typedef struct sf_state_report {
 } sf_state_report;
 SF_API sf_status sf_check_state(sf_ctx* ctx, sf_state_report* report);
 
+/* ---- fault injection (tests) ---------------------------------------------
+ * The device allocation `after` allocations from now (0: the next one) fails
+ * as out of memory, once; a negative value disarms it.  The call that hits it
+ * returns SF_ERR_OUT_OF_MEMORY and releases what it had allocated: the
+ * context stays usable and may need a new sf_set_state. */
+SF_API sf_status sf_test_fail_allocation(int64_t after);
+
 /* ---- kernel tuning -----------------------------------------------------------
  * Implementation choices of a context's step.  Every choice computes the same
  * bits; they differ only in speed.  Not part of the reference interface. */

@@ -143,6 +143,7 @@ PROTOTYPES = {
     "sf_get_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
     "sf_device_state": (c_int32, [c_void_p, _P(sf_device_view)]),
     "sf_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
+    "sf_test_fail_allocation": (c_int32, [ctypes.c_int64]),
     "sf_batch_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
     "sf_get_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
     "sf_make_ready": (c_int32, [c_void_p]),

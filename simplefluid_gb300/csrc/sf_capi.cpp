@@ -8,6 +8,7 @@
 //   getParticles()/getVelocity()    Include/QtSPHSolver.h:34-35   -> sf_get_state / sf_set_state
 //   SceneManager::setupScene        Source/SceneManager.cpp:21-38 -> sf_setup_scene
 //   SPHParameters::updateParams()   Source/Controller.cpp:63      -> sf_params_update
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -15,6 +16,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "sf_internal.h"
 #include "sf_render.h"
@@ -88,7 +90,37 @@ struct sf_ctx {
 
 namespace {
 
+// NVTX range over an API call (visible in Nsight timelines; a no-op without a
+// tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define SF_RANGE(name) NvtxRange sf_nvtx_range_(name)
+
 thread_local std::string g_error;
+
+// Fault injection (sf_test_fail_allocation): device allocations to let
+// through before one fails as out of memory; negative when disarmed.
+std::atomic<int64_t> g_fail_alloc{-1};
+
+cudaError_t dev_malloc_raw(void** p, size_t bytes) {
+    int64_t k = g_fail_alloc.load();
+    while (k >= 0 && !g_fail_alloc.compare_exchange_weak(k, k - 1)) {
+    }
+    if (k == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+template <typename T>
+cudaError_t dev_malloc(T** p, size_t bytes) {
+    return dev_malloc_raw(reinterpret_cast<void**>(p), bytes);
+}
 
 sf_status fail(sf_status st, const std::string& msg) {
     g_error = msg;
@@ -261,41 +293,58 @@ void drop_graph(sf_ctx* ctx) {
     ++ctx->gen;
 }
 
+// On any failure the grid is released and the context needs a new upload.
 sf_status alloc_grid(sf_ctx* ctx) {
     sf::DeviceState& d = ctx->d;
     if (d.ncells == ctx->c.ncells && d.counts) return SF_OK;
     free_grid(d);
     const uint64_t pad = ((uint64_t)ctx->c.ncells + 1 + sf::kScanTile - 1) / sf::kScanTile * sf::kScanTile;
+    const uint32_t ntiles = (uint32_t)(pad / sf::kScanTile);
+    cudaError_t e = dev_malloc(&d.counts, pad * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.cell_start, pad * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.tile_sums, (size_t)ntiles * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.tile_sums, 0, (size_t)ntiles * sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.counts, 0, pad * sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_start, 0, pad * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) {
+        free_grid(d);
+        ctx->sorted = false;
+        return cuda_fail(e, "grid allocation");
+    }
     d.ncells = ctx->c.ncells;
     d.ncells_pad = (uint32_t)pad;
-    d.ntiles = (uint32_t)(pad / sf::kScanTile);
-    SF_CUDA(cudaMalloc(&d.counts, pad * sizeof(uint32_t)));
-    SF_CUDA(cudaMalloc(&d.cell_start, pad * sizeof(uint32_t)));
-    SF_CUDA(cudaMalloc(&d.tile_sums, (size_t)d.ntiles * sizeof(uint32_t)));
-    SF_CUDA(cudaMemsetAsync(d.tile_sums, 0, (size_t)d.ntiles * sizeof(uint32_t), ctx->stream));
-    SF_CUDA(cudaMemsetAsync(d.counts, 0, pad * sizeof(uint32_t), ctx->stream));
-    SF_CUDA(cudaMemsetAsync(d.cell_start, 0, pad * sizeof(uint32_t), ctx->stream));
+    d.ntiles = ntiles;
     return SF_OK;
 }
 
+// On any failure the particle buffers are released and the context holds no
+// particles until the next successful upload.
 sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     sf::DeviceState& d = ctx->d;
     if (n <= d.cap && d.pos) return SF_OK;
+    free_trajectory(ctx);  // its buffers are sized by the capacity
     free_particles(d);
     const size_t c = n ? n : 1;
-    SF_CUDA(cudaMalloc(&d.pos, c * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&d.vel, c * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&d.pos2, c * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&d.vel2, c * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&d.pr, c * sizeof(float2)));
-    SF_CUDA(cudaMalloc(&d.rho, c * sizeof(float)));
-    SF_CUDA(cudaMalloc(&d.key_slot, c * sizeof(uint2)));
-    SF_CUDA(cudaMalloc(&d.tmp, c * sizeof(uint32_t)));
-    SF_CUDA(cudaMalloc(&d.io, c * 6 * sizeof(float)));
     const size_t tiles = (c + sf::kNbTile - 1) / sf::kNbTile;
-    SF_CUDA(cudaMalloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t)));
-    SF_CUDA(cudaMalloc(&d.nbr_count, c * sizeof(uint32_t)));
-    SF_CUDA(cudaMemset(d.nbr_count, 0, c * sizeof(uint32_t)));
+    cudaError_t e = dev_malloc(&d.pos, c * sizeof(float4));
+    if (e == cudaSuccess) e = dev_malloc(&d.vel, c * sizeof(float4));
+    if (e == cudaSuccess) e = dev_malloc(&d.pos2, c * sizeof(float4));
+    if (e == cudaSuccess) e = dev_malloc(&d.vel2, c * sizeof(float4));
+    if (e == cudaSuccess) e = dev_malloc(&d.pr, c * sizeof(float2));
+    if (e == cudaSuccess) e = dev_malloc(&d.rho, c * sizeof(float));
+    if (e == cudaSuccess) e = dev_malloc(&d.key_slot, c * sizeof(uint2));
+    if (e == cudaSuccess) e = dev_malloc(&d.tmp, c * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.io, c * 6 * sizeof(float));
+    if (e == cudaSuccess) e = dev_malloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.nbr_count, c * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(d.nbr_count, 0, c * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        free_particles(d);
+        d.n = 0;
+        ctx->sorted = false;
+        drop_graph(ctx);
+        return cuda_fail(e, "particle buffer allocation");
+    }
     d.cap = (uint32_t)c;
     return SF_OK;
 }
@@ -656,7 +705,7 @@ SF_API sf_status sf_create(const sf_params* p, sf_ctx** out) {
     }
     st = alloc_grid(ctx);
     if (!st) {
-        e = cudaMalloc(&ctx->frame, sizeof(sf::FrameState));
+        e = dev_malloc(&ctx->frame, sizeof(sf::FrameState));
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->frame, 0, sizeof(sf::FrameState), ctx->stream);
         if (e != cudaSuccess) st = cuda_fail(e, "frame state");
     }
@@ -749,6 +798,7 @@ SF_API sf_status sf_get_params(const sf_ctx* ctx, sf_params* p) {
 }
 
 SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz, uint32_t n) {
+    SF_RANGE("sf_set_state");
     SF_TRY(need_ctx(ctx));
     if (n && !pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null positions");
     SF_TRY(set_device(ctx));
@@ -780,6 +830,7 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
 }
 
 SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint32_t n) {
+    SF_RANGE("sf_get_state");
     SF_TRY(need_sorted(ctx));
     if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
     SF_TRY(set_device(ctx));
@@ -838,6 +889,7 @@ sf_status stream_after(cudaStream_t waiter, cudaStream_t signaller) {
 
 SF_API sf_status sf_set_state_device(sf_ctx* ctx, const float* d_pos_xyz, const float* d_vel_xyz, uint32_t n,
                                      void* other) {
+    SF_RANGE("sf_set_state_device");
     SF_TRY(need_ctx(ctx));
     if (n && !d_pos_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "null positions");
     SF_TRY(set_device(ctx));
@@ -854,6 +906,7 @@ SF_API sf_status sf_set_state_device(sf_ctx* ctx, const float* d_pos_xyz, const 
 }
 
 SF_API sf_status sf_get_state_device(sf_ctx* ctx, float* d_pos_xyz, float* d_vel_xyz, uint32_t n, void* other) {
+    SF_RANGE("sf_get_state_device");
     SF_TRY(need_sorted(ctx));
     if (n != ctx->d.n) return fail(SF_ERR_INVALID_ARGUMENT, "n does not match the number of particles");
     SF_TRY(set_device(ctx));
@@ -880,6 +933,7 @@ SF_API sf_status sf_device_state(sf_ctx* ctx, sf_device_view* view) {
 }
 
 SF_API sf_status sf_make_ready(sf_ctx* ctx) {
+    SF_RANGE("sf_make_ready");
     SF_TRY(need_sorted(ctx));
     SF_TRY(set_device(ctx));
     if (!ctx->step_graph) SF_TRY(capture_step(ctx));
@@ -940,6 +994,7 @@ static sf_status build_frame_graph(sf_ctx* ctx, double frame_time, uint32_t max_
 
 SF_API sf_status sf_advance_frames(sf_ctx* ctx, uint32_t frames, double frame_time, uint32_t max_substeps,
                                    double* sim_time_out, uint32_t* substeps_out) {
+    SF_RANGE("sf_advance_frames");
     SF_TRY(sf_make_ready(ctx));
     if (!(frame_time > 0.0) || max_substeps == 0) return fail(SF_ERR_INVALID_ARGUMENT, "need frame_time > 0, max_substeps > 0");
     if (!ctx->frame_graph || ctx->frame_graph_gen != ctx->gen || ctx->frame_graph_time != frame_time ||
@@ -963,6 +1018,7 @@ SF_API sf_status sf_advance_frames(sf_ctx* ctx, uint32_t frames, double frame_ti
 }
 
 SF_API sf_status sf_step(sf_ctx* ctx, uint32_t nsteps) {
+    SF_RANGE("sf_step");
     SF_TRY(sf_make_ready(ctx));
     for (uint32_t s = 0; s < nsteps; ++s) SF_CUDA(cudaGraphLaunch(ctx->step_graph, ctx->stream));
     return SF_OK;
@@ -1056,7 +1112,7 @@ SF_API sf_status sf_compute_accel(sf_ctx* ctx, float* accel_xyz, uint32_t n) {
     SF_TRY(need_sorted(ctx));
     if (n != ctx->d.n || !accel_xyz) return fail(SF_ERR_INVALID_ARGUMENT, "bad output or size");
     SF_TRY(set_device(ctx));
-    if (!ctx->d.accel) SF_CUDA(cudaMalloc(&ctx->d.accel, (size_t)ctx->d.cap * sizeof(float4)));
+    if (!ctx->d.accel) SF_CUDA(dev_malloc(&ctx->d.accel, (size_t)ctx->d.cap * sizeof(float4)));
     sf::launch_density(ctx->d, ctx->c, ctx->stream);
     sf::launch_force_only(ctx->d, ctx->c, ctx->stream);
     SF_TRY(check_launch("forces"));
@@ -1084,11 +1140,17 @@ SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash
     return SF_OK;
 }
 
+SF_API sf_status sf_test_fail_allocation(int64_t after) {
+    g_fail_alloc.store(after < 0 ? -1 : after);
+    return SF_OK;
+}
+
 SF_API sf_status sf_check_state(sf_ctx* ctx, sf_state_report* report) {
+    SF_RANGE("sf_check_state");
     SF_TRY(need_sorted(ctx));
     if (!report) return fail(SF_ERR_INVALID_ARGUMENT, "null output");
     SF_TRY(set_device(ctx));
-    if (!ctx->d_report) SF_CUDA(cudaMalloc(&ctx->d_report, sf::kReportWords * sizeof(uint32_t)));
+    if (!ctx->d_report) SF_CUDA(dev_malloc(&ctx->d_report, sf::kReportWords * sizeof(uint32_t)));
     // the bucketed-index buffer is free between steps: it holds the id tally
     const bool lists = ctx->d.nbr && ctx->d.tune.list_mode != SF_LIST_NONE;
     sf::launch_check_state(ctx->d, ctx->c, lists ? ctx->d.nbr_count : nullptr, ctx->d.tmp, ctx->d_report,
@@ -1144,7 +1206,7 @@ SF_API sf_status sf_step_timed(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_byte
     *total_ms = 0.f;
     if (!nsteps) return SF_OK;
     Scratch flush;
-    if (flush_bytes) SF_CUDA(cudaMalloc(&flush.p, flush_bytes));
+    if (flush_bytes) SF_CUDA(dev_malloc(&flush.p, flush_bytes));
     EventSet ev;
     SF_CUDA(ev.create(2 * (size_t)nsteps));
     for (uint32_t i = 0; i < nsteps; ++i) {
@@ -1208,7 +1270,7 @@ SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_b
     for (uint32_t s = 0; s < nstages; ++s) stage_ms[s] = 0.f;
     if (!nsteps) return SF_OK;
     Scratch flush;
-    if (flush_bytes) SF_CUDA(cudaMalloc(&flush.p, flush_bytes));
+    if (flush_bytes) SF_CUDA(dev_malloc(&flush.p, flush_bytes));
     const size_t per = (size_t)sf::kNumStages + 1;
     EventSet ev;
     SF_CUDA(ev.create(per * nsteps));
@@ -1288,6 +1350,7 @@ SF_API sf_status sf_render_params_default(sf_render_params* rp) {
 
 SF_API sf_status sf_render(sf_ctx* ctx, const sf_render_params* rp, float* rgba_out, float* depth_out,
                            uint32_t* owner_out) {
+    SF_RANGE("sf_render");
     SF_TRY(need_sorted(ctx));
     if (!rp) return fail(SF_ERR_INVALID_ARGUMENT, "null render parameters");
     if (rp->width <= 0 || rp->height <= 0 || (int64_t)rp->width * rp->height > (1 << 26))
@@ -1302,11 +1365,11 @@ SF_API sf_status sf_render(sf_ctx* ctx, const sf_render_params* rp, float* rgba_
     if (ctx->render_w != rp->width || ctx->render_h != rp->height || ctx->render_n < ctx->d.cap) {
         free_render(ctx);
         const size_t np = (size_t)rp->width * rp->height;
-        SF_CUDA(cudaMalloc(&ctx->render_keys, np * sizeof(unsigned long long)));
-        SF_CUDA(cudaMalloc(&ctx->render_rgba, np * sizeof(float4)));
-        SF_CUDA(cudaMalloc(&ctx->render_depth, np * sizeof(float)));
-        SF_CUDA(cudaMalloc(&ctx->render_owner, np * sizeof(uint32_t)));
-        SF_CUDA(cudaMalloc(&ctx->render_slot, (size_t)ctx->d.cap * sizeof(uint32_t)));
+        SF_CUDA(dev_malloc(&ctx->render_keys, np * sizeof(unsigned long long)));
+        SF_CUDA(dev_malloc(&ctx->render_rgba, np * sizeof(float4)));
+        SF_CUDA(dev_malloc(&ctx->render_depth, np * sizeof(float)));
+        SF_CUDA(dev_malloc(&ctx->render_owner, np * sizeof(uint32_t)));
+        SF_CUDA(dev_malloc(&ctx->render_slot, (size_t)ctx->d.cap * sizeof(uint32_t)));
         ctx->render_w = rp->width;
         ctx->render_h = rp->height;
         ctx->render_n = ctx->d.cap;
@@ -1332,6 +1395,7 @@ SF_API sf_status sf_render(sf_ctx* ctx, const sf_render_params* rp, float* rgba_
 // The n x 3 arrays can be read directly for offline use; particle i of the
 // caller's order is at the row whose index entry is i.
 SF_API sf_status sf_save_state(sf_ctx* ctx, const char* path, double sim_time) {
+    SF_RANGE("sf_save_state");
     SF_TRY(need_sorted(ctx));
     if (!path) return fail(SF_ERR_INVALID_ARGUMENT, "null path");
     SF_TRY(set_device(ctx));
@@ -1357,6 +1421,7 @@ SF_API sf_status sf_save_state(sf_ctx* ctx, const char* path, double sim_time) {
 }
 
 SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_out) {
+    SF_RANGE("sf_load_state");
     SF_TRY(need_ctx(ctx));
     if (!path) return fail(SF_ERR_INVALID_ARGUMENT, "null path");
     FILE* f = std::fopen(path, "rb");
@@ -1450,7 +1515,7 @@ sf_status batch_derive(sf_batch* b, int K) {
 
 sf_status batch_upload_table(sf_batch* b) {
     const size_t ns = b->consts.size();
-    if (!b->d_table) SF_CUDA(cudaMalloc(&b->d_table, ns * sizeof(sf::SimConst)));
+    if (!b->d_table) SF_CUDA(dev_malloc(&b->d_table, ns * sizeof(sf::SimConst)));
     SF_CUDA(cudaMemcpyAsync(b->d_table, b->consts.data(), ns * sizeof(sf::SimConst), cudaMemcpyHostToDevice,
                             b->eng.stream));
     SF_CUDA(cudaStreamSynchronize(b->eng.stream));
@@ -1515,7 +1580,7 @@ SF_API sf_status sf_batch_create(const sf_params* per_scene, uint32_t nscenes, s
     }
     cudaError_t e = cudaGetDevice(&b->eng.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->eng.stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_off, (nscenes + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&b->d_off, (nscenes + 1) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_off, 0, (nscenes + 1) * sizeof(uint32_t), b->eng.stream);
     if (e != cudaSuccess) {
         sf_batch_destroy(b);
@@ -1641,6 +1706,7 @@ SF_API sf_status sf_batch_set_cells_per_h(sf_batch* b, int32_t cells_per_h) {
 // order (and so the last bits); the kernel variants do not.
 SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning* chosen, int32_t* chosen_cells_per_h,
                                    float* chosen_ms_per_step) {
+    SF_RANGE("sf_batch_autotune");
     SF_TRY(need_batch(b));
     SF_TRY(need_sorted(&b->eng));
     if (trial_steps == 0) return fail(SF_ERR_INVALID_ARGUMENT, "trial_steps must be > 0");
@@ -1693,22 +1759,33 @@ SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning*
 // ---------------------------------------------------------------- adjoint
 namespace {
 
+// A failed trajectory allocation releases the whole trajectory, so that no
+// partly allocated record set is ever used.
+#define SF_ALLOC_TRAJ(ptr, bytes)                                  \
+    do {                                                           \
+        const cudaError_t e_ = dev_malloc(&(ptr), (bytes));        \
+        if (e_ != cudaSuccess) {                                   \
+            free_trajectory(ctx);                                  \
+            return cuda_fail(e_, "trajectory allocation");         \
+        }                                                          \
+    } while (0)
+
 sf_status ensure_work(sf_ctx* ctx) {
     sf::Trajectory* t = ctx->traj;
     const size_t n = ctx->d.cap;
     sf::AdjointWork& w = t->w;
     if (w.Xb) return SF_OK;
-    SF_CUDA(cudaMalloc(&w.Xb, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.Vb, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.apb, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.avb, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.xdir, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.vdir, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.xf, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.vf, n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&w.rhob, n * sizeof(float)));
-    SF_CUDA(cudaMalloc(&w.scalars, 2 * sizeof(double)));
-    SF_CUDA(cudaMalloc(&t->snap, 2 * n * sizeof(float4)));
+    SF_ALLOC_TRAJ(w.Xb, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.Vb, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.apb, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.avb, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.xdir, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.vdir, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.xf, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.vf, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.rhob, n * sizeof(float));
+    SF_ALLOC_TRAJ(w.scalars, 2 * sizeof(double));
+    SF_ALLOC_TRAJ(t->snap, 2 * n * sizeof(float4));
     return SF_OK;
 }
 
@@ -1723,19 +1800,19 @@ sf_status ensure_records(sf_ctx* ctx, uint32_t ckpt) {
     if (t->seg_partial) cudaFree(t->seg_partial);
     t->stage = nullptr;
     t->seg_partial = nullptr;
-    SF_CUDA(cudaMalloc(&t->stage, 2 * n * sizeof(float4)));
-    SF_CUDA(cudaMalloc(&t->seg_partial, (size_t)ckpt * sf::adjoint_partial_count((uint32_t)n) * sizeof(double2)));
+    SF_ALLOC_TRAJ(t->stage, 2 * n * sizeof(float4));
+    SF_ALLOC_TRAJ(t->seg_partial, (size_t)ckpt * sf::adjoint_partial_count((uint32_t)n) * sizeof(double2));
     t->rec.assign(ckpt, sf::StepRec{});
     t->ncells_pad = ctx->d.ncells_pad;
     for (auto& r : t->rec) {
-        SF_CUDA(cudaMalloc(&r.pos, n * sizeof(float4)));
-        SF_CUDA(cudaMalloc(&r.vel, n * sizeof(float4)));
-        SF_CUDA(cudaMalloc(&r.pr, n * sizeof(float2)));
-        SF_CUDA(cudaMalloc(&r.rho, n * sizeof(float)));
-        SF_CUDA(cudaMalloc(&r.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t)));
-        SF_CUDA(cudaMalloc(&r.cnt, n * sizeof(uint32_t)));
-        SF_CUDA(cudaMalloc(&r.cs, (size_t)ctx->d.ncells_pad * sizeof(uint32_t)));
-        SF_CUDA(cudaMalloc(&r.sums, 2 * n * sizeof(float4)));
+        SF_ALLOC_TRAJ(r.pos, n * sizeof(float4));
+        SF_ALLOC_TRAJ(r.vel, n * sizeof(float4));
+        SF_ALLOC_TRAJ(r.pr, n * sizeof(float2));
+        SF_ALLOC_TRAJ(r.rho, n * sizeof(float));
+        SF_ALLOC_TRAJ(r.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t));
+        SF_ALLOC_TRAJ(r.cnt, n * sizeof(uint32_t));
+        SF_ALLOC_TRAJ(r.cs, (size_t)ctx->d.ncells_pad * sizeof(uint32_t));
+        SF_ALLOC_TRAJ(r.sums, 2 * n * sizeof(float4));
     }
     return SF_OK;
 }
@@ -1863,6 +1940,7 @@ sf_status segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
 extern "C" {
 
 SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every) {
+    SF_RANGE("sf_forward");
     SF_TRY(sf_make_ready(ctx));
     if (ctx->c.adaptive) return fail(SF_ERR_INVALID_ARGUMENT, "differentiation needs a fixed time step");
     if (ckpt_every == 0) return fail(SF_ERR_INVALID_ARGUMENT, "ckpt_every must be > 0");
@@ -1870,11 +1948,13 @@ SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every) {
     sf::Trajectory* t = ctx->traj;
     sf::DeviceState& d = ctx->d;
     const uint32_t nck = (nsteps + ckpt_every - 1) / ckpt_every;
+    t->valid = false;
     if (t->n != d.cap || t->ck.size() != nck) {
         for (float4* p : t->ck)
             if (p) cudaFree(p);
         t->ck.assign(nck, nullptr);
-        for (auto& p : t->ck) SF_CUDA(cudaMalloc(&p, 2 * (size_t)d.cap * sizeof(float4)));
+        t->n = 0;
+        for (auto& p : t->ck) SF_ALLOC_TRAJ(p, 2 * (size_t)d.cap * sizeof(float4));
     }
     t->valid = false;
     for (uint32_t s = 0; s < nsteps; ++s) {
@@ -1894,6 +1974,7 @@ SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every) {
 }
 
 SF_API sf_status sf_loss_histogram(sf_ctx* ctx, const float* target, uint32_t res, double* loss_out, float* dloss_dx) {
+    SF_RANGE("sf_loss_histogram");
     SF_TRY(need_sorted(ctx));
     if (!target || res == 0 || res > 1024 || !loss_out) return fail(SF_ERR_INVALID_ARGUMENT, "bad target or resolution");
     SF_TRY(set_device(ctx));
@@ -1909,10 +1990,10 @@ SF_API sf_status sf_loss_histogram(sf_ctx* ctx, const float* target, uint32_t re
         t->hist = nullptr;
         t->e2 = t->target = nullptr;
         t->hpartial = nullptr;
-        SF_CUDA(cudaMalloc(&t->hist, nc * sizeof(unsigned long long)));
-        SF_CUDA(cudaMalloc(&t->e2, nc * sizeof(float)));
-        SF_CUDA(cudaMalloc(&t->target, nc * sizeof(float)));
-        SF_CUDA(cudaMalloc(&t->hpartial, sf::histogram_partial_count(res) * sizeof(double)));
+        SF_ALLOC_TRAJ(t->hist, nc * sizeof(unsigned long long));
+        SF_ALLOC_TRAJ(t->e2, nc * sizeof(float));
+        SF_ALLOC_TRAJ(t->target, nc * sizeof(float));
+        SF_ALLOC_TRAJ(t->hpartial, sf::histogram_partial_count(res) * sizeof(double));
         t->hist_res = res;
     }
     SF_TRY(copy_in(ctx, t->target, target, nc * sizeof(float)));
@@ -1931,6 +2012,7 @@ SF_API sf_status sf_loss_histogram(sf_ctx* ctx, const float* target, uint32_t re
 
 SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dloss_dv, float* dloss_dx0,
                             float* dloss_dv0, float* dloss_dviscosity, float* dloss_dstiffness) {
+    SF_RANGE("sf_adjoint");
     SF_TRY(need_sorted(ctx));
     sf::Trajectory* t = ctx->traj;
     if (!t || !t->valid || t->n != ctx->d.cap) return fail(SF_ERR_NOT_READY, "no recorded trajectory: call sf_forward");
