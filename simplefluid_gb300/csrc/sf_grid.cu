@@ -183,19 +183,33 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_totals(const uint4* __res
 // Exclusive scan of the cell histogram into the cell table.  Block b scans
 // tile b (kScanTile cells) and adds the totals of tiles 0..b-1, which the
 // histogram atomics accumulated in tile_sums, so one kernel does the whole scan.
+// The predecessor sum and the tile's scan share one two-barrier pass.
 __global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__ counts,
                                                        const uint32_t* __restrict__ tile_sums,
                                                        uint4* __restrict__ cell_start) {
+    static_assert(kScanThreads == 1024, "one warp-sum slot per warp");
     grid_dependency_wait();
     allow_dependents();
-    __shared__ uint32_t total;
-    uint32_t before = 0;
-    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += kScanThreads) before += tile_sums[t];
-    block_exclusive(before, &total);
-    const uint32_t offset = total;
+    __shared__ uint32_t s_warp[32], s_before[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t t = (size_t)blockIdx.x * kScanThreads + threadIdx.x;
     const uint4 q = counts[t];
-    const uint32_t ex = block_exclusive(q.x + q.y + q.z + q.w, &total) + offset;
+    uint32_t before = 0;
+    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += kScanThreads) before += tile_sums[k];
+    const uint32_t v = q.x + q.y + q.z + q.w;
+    const uint32_t inc = warp_inclusive(v);
+    before = __reduce_add_sync(0xffffffffu, before);
+    if (lane == 31) s_warp[warp] = inc;
+    if (lane == 0) s_before[warp] = before;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = s_warp[lane];
+        const uint32_t wi = warp_inclusive(w);
+        const uint32_t b = __reduce_add_sync(0xffffffffu, s_before[lane]);
+        s_warp[lane] = wi - w + b;  // cells of the earlier warps and tiles
+    }
+    __syncthreads();
+    const uint32_t ex = s_warp[warp] + inc - v;
     cell_start[t] = make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
 }
 
