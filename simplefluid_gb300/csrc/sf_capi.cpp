@@ -220,7 +220,8 @@ bool is_pinned(const void* p) {
 }
 
 void free_particles(sf::DeviceState& d) {
-    void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel, d.nbr, d.nbr_count};
+    void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel, d.nbr, d.nbr_count,
+                    d.pv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     d.pos = d.vel = d.pos2 = d.vel2 = d.accel = nullptr;
@@ -231,6 +232,7 @@ void free_particles(sf::DeviceState& d) {
     d.io = nullptr;
     d.nbr = nullptr;
     d.nbr_count = nullptr;
+    d.pv = nullptr;
     d.cap = 0;
 }
 
@@ -337,6 +339,7 @@ sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     if (e == cudaSuccess) e = dev_malloc(&d.io, c * 6 * sizeof(float));
     if (e == cudaSuccess) e = dev_malloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t));
     if (e == cudaSuccess) e = dev_malloc(&d.nbr_count, c * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.pv, c * 2 * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemset(d.nbr_count, 0, c * sizeof(uint32_t));
     if (e != cudaSuccess) {
         free_particles(d);

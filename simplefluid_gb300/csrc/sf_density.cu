@@ -3,8 +3,10 @@
 // One thread per cell-sorted particle.  Poly6 density over the canonical
 // candidates; non-neighbours add an exact zero (fma(0, 0, s) == s), so the sum
 // is branch-free and bit-identical to summing neighbours only.  The pass also
-// evaluates the equation of state and records each particle's neighbours
-// (itself included, in its canonical place) for the force pass:
+// evaluates the equation of state, writes each particle's 32-byte record for
+// the force pass's gathers ((x, y, z, p), (vx, vy, vz, 1/rho)), and records
+// each particle's neighbours (itself included, in its canonical place) for the
+// force pass:
 //   kEmitNone    no list (the force pass rescans the candidate cells);
 //   kEmitStaged  list staged in shared memory, written out in full lines;
 //   kEmitTile    list written directly.
@@ -23,7 +25,7 @@ __global__ void __launch_bounds__(kBlockSize)
     k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n, SimConst c0,
               const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
               float* __restrict__ rho_out, float2* __restrict__ pr_out, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count) {
+              uint32_t* __restrict__ nbr_count, const float4* __restrict__ vel, float4* __restrict__ pv) {
     __shared__ uint32_t s_nb[kMode == kEmitStaged ? kNbCap : 1][kMode == kEmitStaged ? kBlockSize : 1];
     grid_dependency_wait();
     allow_dependents();
@@ -49,8 +51,13 @@ __global__ void __launch_bounds__(kBlockSize)
             }
         });
         const float rho = c.cd * s;
+        const float p = pressure_of(c, rho), inv_rho = 1.f / rho;
         rho_out[i] = rho;
-        pr_out[i] = make_float2(pressure_of(c, rho), 1.f / rho);
+        pr_out[i] = make_float2(p, inv_rho);
+        if (kMode != kEmitNone) {
+            const float4 v = vel[i];
+            st8(pv + 2 * (size_t)i, make_float4(xi.x, xi.y, xi.z, p), make_float4(v.x, v.y, v.z, inv_rho));
+        }
         if (kMode != kEmitNone) nbr_count[i] = cnt;
     }
     if (kMode == kEmitStaged) {
@@ -69,10 +76,10 @@ void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
             if constexpr (K <= 2)
                 launch_chained(k_density<kMode, kBlockSize, K, true>, grid_for(d.n, kBlockSize), kBlockSize, s,
                                d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, d.rho, d.pr, d.nbr,
-                               d.nbr_count);
+                               d.nbr_count, d.vel, d.pv);
         } else {
             launch_chained(k_density<kMode, kBlockSize, K, false>, grid_for(d.n, kBlockSize), kBlockSize, s, d.pos,
-                           d.cell_start, d.n, c, nullptr, nullptr, 0u, d.rho, d.pr, d.nbr, d.nbr_count);
+                           d.cell_start, d.n, c, nullptr, nullptr, 0u, d.rho, d.pr, d.nbr, d.nbr_count, d.vel, d.pv);
         }
     });
 }

@@ -236,6 +236,18 @@ __device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const u
     }
 }
 
+// One 32-byte record in one access (sm_100+ 256-bit vector load / store).
+__device__ __forceinline__ void ld8(const float4* __restrict__ p, float4& a, float4& b) {
+    asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
+__device__ __forceinline__ void st8(float4* __restrict__ p, const float4& a, const float4& b) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
+
 // Equation of state and the p >= 0 clamp (SPHParameters::bUseAttractivePressure).
 __device__ __forceinline__ float pressure_of(const SimConst& c, float rho) {
     float p;

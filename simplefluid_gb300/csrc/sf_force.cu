@@ -6,6 +6,8 @@
 // where the list overflowed or no list was recorded — then, in the stepping
 // variant, symplectic Euler, the box clamp with restitution and the next
 // step's cell key and arrival slot (the counting sort's histogram).
+// A neighbour on the list is one 32-byte record written by the density pass,
+// (x, y, z, p) and (vx, vy, vz, 1/rho), fetched with one 256-bit load.
 // kPrefetch neighbours are gathered before their terms are added, and the
 // next kPrefetch list indices are loaded while they are, so the dependent
 // index -> data loads of consecutive batches overlap; the terms are still
@@ -22,7 +24,7 @@ template <bool kUseList, int kPrefetch, bool kIntegrate, int kReach, bool kBatch
 __device__ __forceinline__ void force_one(
     uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-    const SimConst& c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
+    const float4* __restrict__ pv, const SimConst& c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint32_t* __restrict__ counts,
     uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
     float4* __restrict__ sums, const FrameState* __restrict__ frame, uint32_t& v2, uint32_t& a2) {
@@ -41,7 +43,6 @@ __device__ __forceinline__ void force_one(
         for (; k + kPrefetch <= cnt; k += kPrefetch) {
             uint32_t j[kPrefetch];
             float4 xj[kPrefetch], vj[kPrefetch];
-            float2 pj[kPrefetch];
 #pragma unroll
             for (int u = 0; u < kPrefetch; ++u) {
                 j[u] = jn[u];
@@ -49,17 +50,16 @@ __device__ __forceinline__ void force_one(
                 jn[u] = __ldg(lst + (size_t)min(k + kPrefetch + u, (uint32_t)kNbCap - 1) * kNbTile);
             }
 #pragma unroll
-            for (int u = 0; u < kPrefetch; ++u) {
-                xj[u] = ldg4(pos + j[u]);
-                vj[u] = ldg4(vel + j[u]);
-                pj[u] = __ldg(pr + j[u]);
-            }
+            for (int u = 0; u < kPrefetch; ++u) ld8(pv + 2 * (size_t)j[u], xj[u], vj[u]);
 #pragma unroll
-            for (int u = 0; u < kPrefetch; ++u) pair_terms(c, xi, vi, pri.x, xj[u], pj[u], vj[u], a);
+            for (int u = 0; u < kPrefetch; ++u)
+                pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
         }
         for (; k < cnt; ++k) {
             const uint32_t j = __ldg(nbr + nbr_index(i, k));
-            pair_terms(c, xi, vi, pri.x, ldg4(pos + j), __ldg(pr + j), ldg4(vel + j), a);
+            float4 xj, vj;
+            ld8(pv + 2 * (size_t)j, xj, vj);
+            pair_terms(c, xi, vi, pri.x, xj, make_float2(xj.w, vj.w), vj, a);
         }
     } else {
         for_candidates_rolled<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
@@ -108,7 +108,7 @@ template <bool kUseList, int kPrefetch, int kBlockSize, bool kIntegrate, int kRe
 __global__ void __launch_bounds__(kBlockSize)
     k_force(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-            uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
+            const float4* __restrict__ pv, uint32_t n, SimConst c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off,
             uint32_t nscenes, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             uint32_t* __restrict__ counts, uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot,
             float4* __restrict__ acc_out, float4* __restrict__ sums, FrameState* __restrict__ frame) {
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kBlockSize)
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     uint32_t v2 = 0u, a2 = 0u;
     if (i < n)
-        force_one<kUseList, kPrefetch, kIntegrate, kReach, kBatched>(i, pos, vel, pr, cs, nbr, nbr_count, c0, table,
+        force_one<kUseList, kPrefetch, kIntegrate, kReach, kBatched>(i, pos, vel, pr, cs, nbr, nbr_count, pv, c0, table,
                                                                      scene_off, nscenes, pos_out, vel_out, counts,
                                                                      tile_sums, key_slot, acc_out, sums, frame, v2, a2);
     if (!kBatched && kIntegrate && frame && c0.adaptive) {
@@ -156,11 +156,11 @@ void force_as(DeviceState& d, const SimConst& c, cudaStream_t s) {
         if (d.table) {
             if constexpr (K <= 2 && kPrefetch == 2)
                 launch_chained(k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, true>, grid_for(d.n, kBlockSize),
-                               kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c, d.table,
+                               kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.pv, d.n, c, d.table,
                                d.scene_off, d.nscenes, po, vo, co, ts, ks, ac, d.sums, (FrameState*)nullptr);
         } else {
             launch_chained(k_force<kUseList, kPrefetch, kBlockSize, kIntegrate, K, false>, grid_for(d.n, kBlockSize),
-                           kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.n, c,
+                           kBlockSize, s, d.pos, d.vel, d.pr, d.cell_start, d.nbr, d.nbr_count, d.pv, d.n, c,
                            (const SimConst*)nullptr, (const uint32_t*)nullptr, 0u, po, vo, co, ts, ks, ac, d.sums,
                            kIntegrate ? d.frame : nullptr);
         }

@@ -83,6 +83,7 @@ struct DeviceState {
     float4* accel = nullptr;    // optional acceleration output (inspection)
     uint32_t* nbr = nullptr;       // neighbour lists, tile-major (kNbCap * kNbTile per tile)
     uint32_t* nbr_count = nullptr; // neighbours of each particle (may exceed kNbCap)
+    float4* pv = nullptr;          // 2 per particle (32 bytes): (x, y, z, p), (vx, vy, vz, 1/rho)
     float4* sums = nullptr;        // optional: per particle (AP, 0), (AV, 0) of the force pass (adjoint recording)
     FrameState* frame = nullptr;   // adaptive sub-steps read dt here and raise the maxima
     // grid
