@@ -237,13 +237,14 @@ __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t
     // the scan-tile totals are zero again for the next histogram
     for (uint32_t t = i; t < ntiles; t += gridDim.x * blockDim.x) tile_sums[t] = 0u;
     if (i >= n) return;
+    const float4 p = pos_in[i], v = vel_in[i];  // in flight while the rank is found
     const uint32_t key = key_slot[i].x;
     const uint32_t b = cell_start[key], e = cell_start[key + 1];
     uint32_t rank = 0;
     for (uint32_t t = b; t < e; ++t) rank += (tmp[t] < i) ? 1u : 0u;
     const uint32_t dst = b + rank;
-    pos_out[dst] = pos_in[i];
-    vel_out[dst] = vel_in[i];
+    pos_out[dst] = p;
+    vel_out[dst] = v;
 }
 
 // ---------------------------------------------------------------- inspection
