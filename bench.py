@@ -159,16 +159,21 @@ def cpu_oracle_rate(pos: np.ndarray, prm, budget_s: float, max_steps: int, warmu
     return pos.shape[0] * steps / dt, steps, O.max_threads()
 
 
-def measure_batched(args) -> dict:
+def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
     """Batched cubes: 256 scenes (counts log-uniform in [2000, 65536], seed
     20171) advanced together (one graph launch per step, autotuned), against
     stepping each scene on its own context, one scene after another, and
-    against all contexts interleaved on their own streams."""
-    from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes
+    against all contexts interleaved on their own streams.  With several ranks
+    the scenes are spread over them (largest first, no communication) and each
+    throughput is all ranks' particle-updates over the slowest rank's time."""
+    from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes, shard_batch
     steps = args.batch_steps
     base = SPHParameters(particleRadius=0.005, kernelRadius=0.02, pressureStiffness=50.0, viscosity=0.01,
                          restDensity=1000.0, timeStep=1e-4, boundaryRestitution=0.1)
     params, counts, pos = batch_cubes(20171, 256, base)
+    total_scenes = len(params)
+    if ws > 1:
+        params, counts, pos, _ = shard_batch(params, counts, pos, rank, ws)
     n = int(counts.sum())
     with SPHBatch(params) as b:
         b.setState(counts, pos)
@@ -179,7 +184,8 @@ def measure_batched(args) -> dict:
         b.step(3)
         b.synchronize()
         ms = b.timedSteps(steps)
-    batched = n * steps / (ms * 1e-3)
+    t_ms, units = aggregate_over_ranks(dist, ms, n * steps)
+    batched = units / (t_ms * 1e-3)
     off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     ctxs = []
     try:
@@ -198,19 +204,21 @@ def measure_batched(args) -> dict:
         for c in ctxs:
             c.step(steps)
             c.synchronize()
-        seq = n * steps / (time.perf_counter() - t0)
+        t_s, u = aggregate_over_ranks(dist, time.perf_counter() - t0, n * steps)
+        seq = u / t_s
         t0 = time.perf_counter()
         for _ in range(steps):
             for c in ctxs:
                 c.step(1)
         for c in ctxs:
             c.synchronize()
-        rr = n * steps / (time.perf_counter() - t0)
+        t_s, u = aggregate_over_ranks(dist, time.perf_counter() - t0, n * steps)
+        rr = u / t_s
     finally:
         for c in ctxs:
             c.close()
     cpu = None
-    if not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline:
         # the CPU oracle over the scenes one after another, on a sample of them
         ups = secs = 0.0
         threads = 1
@@ -223,7 +231,8 @@ def measure_batched(args) -> dict:
             secs += (off[s + 1] - off[s]) * st / rate
         cpu = {"value": ups / secs, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"scenes {list(sample)} one after another, up to 20 sub-steps each (after 1 warm-up)"}
-    return {"value": batched, "unit": UNIT, "scenes": len(params), "particles": n, "steps": steps,
+    return {"value": batched, "unit": UNIT, "scenes": total_scenes, "particles": units // steps, "steps": steps,
+            "ranks": ws,
             "sequential_value": seq, "ratio_vs_sequential": batched / seq, "interleaved_streams_value": rr,
             "cpu_baseline": cpu,
             "autotuned": {"cells_per_h": K, "list_mode": tune.list_mode, "density_block": tune.density_block,
@@ -465,7 +474,7 @@ def run_ours(args, workload):
                          f"CPU oracle with {threads} OpenMP threads; reference TBB solver library unavailable"}
 
     solver.close()
-    batched = measure_batched(args) if (rank == 0 and not args.no_batched) else None
+    batched = measure_batched(args, dist, rank, ws) if not args.no_batched else None
     adjoint = measure_adjoint(args) if (rank == 0 and not args.no_adjoint) else None
     others = measure_other_workloads(args, workload) if (rank == 0 and not args.no_other_workloads) else None
     if rank != 0:

@@ -5,6 +5,7 @@ The compute lives in the in-tree CUDA library ``_lib/libsimplefluid_gb300.so``
 reference's ``SPHParameters`` / ``SPHSolver`` / ``SceneManager`` / ``Simulator``.
 """
 from ._capi import SFError, load  # noqa: F401
+from .sharding import assign_scenes, shard_batch  # noqa: F401
 from .solver import (  # noqa: F401
     FRAME_TIME,
     SPHBatch,
@@ -20,5 +21,5 @@ from .solver import (  # noqa: F401
     substeps_per_frame,
 )
 
-__all__ = ["render_params", "save_ppm", "read_state_file", "SPHBatch", "batch_cubes", "SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
+__all__ = ["assign_scenes", "shard_batch", "render_params", "save_ppm", "read_state_file", "SPHBatch", "batch_cubes", "SFError", "SceneManager", "Simulator", "SPHParameters", "SPHSolver", "scene_positions",
            "substeps_per_frame", "FRAME_TIME", "load"]
