@@ -62,7 +62,7 @@ int batch_cubes(uint64_t seed, uint32_t nscenes, const sf_params& base, std::vec
 // Kernel choices of a context (all give bit-identical results).
 struct Tuning {
     int list_mode = SF_LIST_TILE;  // SF_LIST_*: how the density pass records neighbours
-    int density_block = 128;       // 128 or 256 threads
+    int density_block = 256;       // 128 or 256 threads
     int force_block = 128;         // 128 or 256 threads
     int prefetch = 2;              // neighbours gathered per batch in the force pass: 2 or 4
 };
