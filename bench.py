@@ -287,6 +287,65 @@ def measure_adjoint(args) -> dict:
                       "adjoint includes the checkpointed forward recompute"}
 
 
+def measure_frames_and_render(args) -> dict:
+    """The reference's frame loop and renderer, each beside the CPU oracle:
+    whole 1/30 s frames with the adaptive sub-step on the device (one graph
+    launch per frame, 16,000-particle dambreak), and the sphere-impostor
+    image of the 1M double dambreak at 1280 x 720 (splat + shade on the
+    device, outputs left in device memory)."""
+    from oracle import oracle as O
+    from simplefluid_gb300 import SPHSolver, render_params, scene_positions
+    from simplefluid_gb300 import _capi as C
+    lib = C.load()
+    out = {}
+    prm = make_params("dambreak_16k")
+    prm.adaptiveTimeStep = True
+    pos = scene_positions(prm, prm.scene)
+    frames = 10
+    with SPHSolver(prm) as s:
+        s.setParticles(pos)
+        s.makeReady()
+        s.advanceFrames(1)
+        s.setParticles(pos)
+        t0 = time.perf_counter()
+        _, sub = s.advanceFrames(frames)
+        gpu_s = time.perf_counter() - t0
+    rec = {"particles": int(pos.shape[0]), "frames": frames, "substeps": int(sub),
+           "frames_per_s": frames / gpu_s, "timing": "wall clock, synchronised"}
+    if not args.no_cpu_baseline:
+        O.build()
+        st = O.State(pos)
+        t0 = time.perf_counter()
+        _, csub, _ = st.frames(prm.to_c(), 1)
+        rec["cpu_baseline"] = {"frames_per_s": 1.0 / (time.perf_counter() - t0), "substeps": int(csub),
+                               "cores": O.max_threads(), "kind": "port", "sample": "the first frame"}
+    out["frames_16k_adaptive"] = rec
+
+    prm = make_params("double_dambreak_1m")
+    pos = scene_positions(prm, prm.scene)
+    rp = render_params(width=1280, height=720, eye=(0.5, 1.3, 2.6), focus=(0.5, 0.3, 0.5))
+    with SPHSolver(prm) as s:
+        s.setParticles(pos)
+        for _ in range(3):
+            C.check(lib.sf_render(s.handle, ctypes.byref(rp), None, None, None))
+        s.synchronize()
+        reps = 20
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            C.check(lib.sf_render(s.handle, ctypes.byref(rp), None, None, None))
+        s.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / reps
+    rec = {"particles": int(pos.shape[0]), "pixels": [1280, 720], "ms_per_image": ms,
+           "timing": "wall clock over 20 images, synchronised"}
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        O.render(prm.to_c(), rp, pos)
+        rec["cpu_baseline"] = {"ms_per_image": (time.perf_counter() - t0) * 1e3, "cores": O.max_threads(),
+                               "kind": "port", "sample": "one image"}
+    out["render_1m_1280x720"] = rec
+    return out
+
+
 def measure_other_workloads(args, skip: str) -> dict:
     """The other single-scene workloads on the GPU (graph-replayed sub-steps,
     CUDA events, L2 flushed before every step) beside the CPU oracle on the
@@ -477,6 +536,8 @@ def run_ours(args, workload):
     batched = measure_batched(args, dist, rank, ws) if not args.no_batched else None
     adjoint = measure_adjoint(args) if (rank == 0 and not args.no_adjoint) else None
     others = measure_other_workloads(args, workload) if (rank == 0 and not args.no_other_workloads) else None
+    if others is not None:
+        others.update(measure_frames_and_render(args))
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
