@@ -13,6 +13,8 @@ namespace sf {
 namespace {
 
 __global__ void k_choose_dt(FrameState* __restrict__ fs, SimConst c) {
+    grid_dependency_wait();
+    allow_dependents();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     float dt = c.dt;
     if (c.adaptive) {
@@ -55,6 +57,8 @@ __global__ void k_frame_begin(FrameState* __restrict__ fs) {
 
 __global__ void k_frame_check(FrameState* __restrict__ fs, double frame_time, uint32_t max_substeps,
                               cudaGraphConditionalHandle h) {
+    grid_dependency_wait();
+    allow_dependents();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const float dt = fs->dt;
     fs->frame_acc = fs->frame_acc + dt;
@@ -66,7 +70,7 @@ __global__ void k_frame_check(FrameState* __restrict__ fs, double frame_time, ui
 
 }  // namespace
 
-void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s) { k_choose_dt<<<1, 32, 0, s>>>(fs, c); }
+void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s) { launch_chained(k_choose_dt, 1, 32, s, fs, c); }
 
 void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s) {
     cudaMemsetAsync(&fs->v2max_bits, 0, 2 * sizeof(uint32_t), s);
@@ -77,7 +81,7 @@ void launch_frame_begin(FrameState* fs, cudaStream_t s) { k_frame_begin<<<1, 32,
 
 void launch_frame_check(FrameState* fs, double frame_time, uint32_t max_substeps, cudaGraphConditionalHandle h,
                         cudaStream_t s) {
-    k_frame_check<<<1, 32, 0, s>>>(fs, frame_time, max_substeps, h);
+    launch_chained(k_frame_check, 1, 32, s, fs, frame_time, max_substeps, h);
 }
 
 }  // namespace sf
