@@ -33,6 +33,9 @@ SOURCES = [
     ("sf_render.cu", ["-fmad=false"]),
     ("sf_frame.cu", ["-fmad=false"]),
     ("sf_capi.cpp", []),
+    ("sf_capi_inspect.cpp", []),
+    ("sf_capi_batch.cpp", []),
+    ("sf_capi_adjoint.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),
 ]
