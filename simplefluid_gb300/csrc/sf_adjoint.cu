@@ -53,13 +53,14 @@ __device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx, f
     return fmaf(az, bz, fmaf(ay, by, ax * bx));
 }
 
-// P1: per sorted particle.  Outputs apb = (cp tb, inv_bar), avb = (cv tb, cv_bar),
-// xdir/vdir = the integration's direct adjoints.
+// P1: per sorted particle.  Outputs the 32-byte record abrec = apb (cp tb,
+// inv_bar), avb (cv tb, cv_bar), and xdir/vdir = the integration's direct
+// adjoints.
 __global__ void __launch_bounds__(kAdjBlock)
     k_adj_integrate(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
                     const float4* __restrict__ sums, uint32_t n, SimConst c, const float4* __restrict__ Xb,
-                    const float4* __restrict__ Vb, float4* __restrict__ apb, float4* __restrict__ avb,
-                    float4* __restrict__ xdir, float4* __restrict__ vdir) {
+                    const float4* __restrict__ Vb, float4* __restrict__ abrec, float4* __restrict__ xdir,
+                    float4* __restrict__ vdir) {
     const uint32_t i = blockIdx.x * kAdjBlock + threadIdx.x;
     if (i >= n) return;
     const float4 x4 = pos[i], v4 = vel[i];
@@ -89,8 +90,8 @@ __global__ void __launch_bounds__(kAdjBlock)
     }
     const float invb = dot3f(ab[0], ab[1], ab[2], t[0], t[1], t[2]);
     const float cvb = dot3f(tb[0], tb[1], tb[2], avs[0], avs[1], avs[2]);
-    apb[i] = make_float4(c.cp * tb[0], c.cp * tb[1], c.cp * tb[2], invb);
-    avb[i] = make_float4(c.cv * tb[0], c.cv * tb[1], c.cv * tb[2], cvb);
+    st8(abrec + 2 * (size_t)i, make_float4(c.cp * tb[0], c.cp * tb[1], c.cp * tb[2], invb),
+        make_float4(c.cv * tb[0], c.cv * tb[1], c.cv * tb[2], cvb));
     xdir[i] = make_float4(xd[0], xd[1], xd[2], 0.f);
     vdir[i] = make_float4(vd[0], vd[1], vd[2], 0.f);
 }
@@ -119,30 +120,32 @@ __device__ __forceinline__ void eos_derivs(const SimConst& c, float rho, float& 
 
 // P2: force pair terms of every pair in both orientations, then the density
 // adjoint of the particle.  Outputs rhob, xf = (force x_bar, k_bar), vf.
+// A neighbour is two 32-byte records, each one 256-bit load: the step's
+// (x, y, z, p | vx, vy, vz, 1/rho) and P1's (apb | avb).
 template <int kReach>
 __global__ void __launch_bounds__(kAdjBlock)
-    k_adj_forces(const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
+    k_adj_forces(const float4* __restrict__ pos, const float4* __restrict__ pv, const float2* __restrict__ pr,
                  const float* __restrict__ rho, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
-                 const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, const float4* __restrict__ apb,
-                 const float4* __restrict__ avb, float* __restrict__ rhob, float4* __restrict__ xf,
-                 float4* __restrict__ vf) {
+                 const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, const float4* __restrict__ ab,
+                 float* __restrict__ rhob, float4* __restrict__ xf, float4* __restrict__ vf) {
     const uint32_t k = blockIdx.x * kAdjBlock + threadIdx.x;
     if (k >= n) return;
-    const float4 xk = pos[k], vk = vel[k];
+    float4 xk, vk, apbk, avbk;
+    ld8(pv + 2 * (size_t)k, xk, vk);
+    ld8(ab + 2 * (size_t)k, apbk, avbk);
     const float2 prk = pr[k];
     const float pk = prk.x, invk = prk.y;
-    const float4 apbk = apb[k], avbk = avb[k];
     float pb = 0.f, invacc = 0.f;
     float xb0 = 0.f, xb1 = 0.f, xb2 = 0.f, vb0 = 0.f, vb1 = 0.f, vb2 = 0.f;
-    for_neighbours<kReach>(c, k, xk, pos, cs, nbr, cnt, [&](uint32_t j, const float4& xj) {
+    for_neighbours<kReach>(c, k, pos[k], pos, cs, nbr, cnt, [&](uint32_t j, const float4&) {
+        float4 xj, vj, apbj, avbj;
+        ld8(pv + 2 * (size_t)j, xj, vj);
+        ld8(ab + 2 * (size_t)j, apbj, avbj);
         const float d0 = xk.x - xj.x, d1 = xk.y - xj.y, d2 = xk.z - xj.z;
         const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
         const float r = sqrtf(r2);
         const float hr = c.h - r;
-        const float2 prj = __ldg(pr + j);
-        const float pj = prj.x, invj = prj.y;
-        const float4 vj = ldg4(vel + j);
-        const float4 apbj = ldg4(apb + j), avbj = ldg4(avb + j);
+        const float pj = xj.w, invj = vj.w;
         const float dv0 = vj.x - vk.x, dv1 = vj.y - vk.y, dv2 = vj.z - vk.z;
         const float ps = pk + pj;
         // orientation A: k is i, j the neighbour
@@ -200,18 +203,18 @@ __global__ void __launch_bounds__(kAdjBlock)
 
 // P4: poly6 density terms onto positions; the step's input adjoints are
 // written back by particle id.
-// Also reduces the step's scalar adjoints (cv_bar in avb.w, k_bar in xf.w) per
+// Also reduces the step's scalar adjoints (cv_bar in avb.w of the ab record, k_bar in xf.w) per
 // block, in thread order, into partial[blockIdx.x].
 template <int kReach>
 __global__ void __launch_bounds__(kAdjBlock)
     k_adj_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
                   const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, float m6cd, const float* __restrict__ rhob,
                   const float4* __restrict__ xdir, const float4* __restrict__ vdir, const float4* __restrict__ xf,
-                  const float4* __restrict__ vf, const float4* __restrict__ avb, float4* __restrict__ Xb,
+                  const float4* __restrict__ vf, const float4* __restrict__ ab, float4* __restrict__ Xb,
                   float4* __restrict__ Vb, double2* __restrict__ partial) {
     __shared__ double s0[kAdjBlock], s1[kAdjBlock];
     const uint32_t k = blockIdx.x * kAdjBlock + threadIdx.x;
-    s0[threadIdx.x] = k < n ? (double)avb[k].w : 0.0;
+    s0[threadIdx.x] = k < n ? (double)ab[2 * (size_t)k + 1].w : 0.0;
     s1[threadIdx.x] = k < n ? (double)xf[k].w : 0.0;
     __syncthreads();
     for (int o = kAdjBlock / 2; o > 0; o >>= 1) {
@@ -385,15 +388,14 @@ void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& 
     const uint32_t n = st.n;
     if (!n) return;
     const unsigned g = grid_for(n, kAdjBlock);
-    k_adj_integrate<<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.sums, n, c, w.Xb, w.Vb, w.apb, w.avb, w.xdir,
-                                            w.vdir);
+    k_adj_integrate<<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.sums, n, c, w.Xb, w.Vb, w.ab, w.xdir, w.vdir);
     const float m6cd = (float)(-6.0 * (double)c.cd);
     with_reach(c.reach, [&](auto R) {
         constexpr int K = decltype(R)::value;
-        k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.apb,
-                                                w.avb, w.rhob, w.xf, w.vf);
+        k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.pv, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.ab,
+                                                w.rhob, w.xf, w.vf);
         k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.rhob, w.xdir, w.vdir,
-                                                 w.xf, w.vf, w.avb, w.Xb, w.Vb, partial);
+                                                 w.xf, w.vf, w.ab, w.Xb, w.Vb, partial);
     });
 }
 

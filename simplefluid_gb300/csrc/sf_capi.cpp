@@ -146,7 +146,7 @@ void free_grid(sf::DeviceState& d) {
 }
 
 void free_rec(sf::StepRec& r) {
-    void* b[] = {r.pos, r.vel, r.pr, r.rho, r.nbr, r.cnt, r.cs, r.sums};
+    void* b[] = {r.pos, r.vel, r.pr, r.rho, r.nbr, r.cnt, r.cs, r.sums, r.pv};
     for (void* p : b)
         if (p) cudaFree(p);
     r = sf::StepRec{};
@@ -169,7 +169,7 @@ void free_trajectory(sf_ctx* ctx) {
     for (float4* p : t->ck)
         if (p) cudaFree(p);
     for (auto& r : t->rec) free_rec(r);
-    void* b[] = {t->snap, t->w.Xb, t->w.Vb, t->w.apb, t->w.avb, t->w.xdir, t->w.vdir, t->w.xf, t->w.vf,
+    void* b[] = {t->snap, t->w.Xb, t->w.Vb, t->w.ab, t->w.xdir, t->w.vdir, t->w.xf, t->w.vf,
                  t->w.rhob, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
     for (void* p : b)
         if (p) cudaFree(p);

@@ -23,8 +23,7 @@ sf_status ensure_work(sf_ctx* ctx) {
     if (w.Xb) return SF_OK;
     SF_ALLOC_TRAJ(w.Xb, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.Vb, n * sizeof(float4));
-    SF_ALLOC_TRAJ(w.apb, n * sizeof(float4));
-    SF_ALLOC_TRAJ(w.avb, n * sizeof(float4));
+    SF_ALLOC_TRAJ(w.ab, 2 * n * sizeof(float4));
     SF_ALLOC_TRAJ(w.xdir, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.vdir, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.xf, n * sizeof(float4));
@@ -59,6 +58,7 @@ sf_status ensure_records(sf_ctx* ctx, uint32_t ckpt) {
         SF_ALLOC_TRAJ(r.cnt, n * sizeof(uint32_t));
         SF_ALLOC_TRAJ(r.cs, (size_t)ctx->d.ncells_pad * sizeof(uint32_t));
         SF_ALLOC_TRAJ(r.sums, 2 * n * sizeof(float4));
+        SF_ALLOC_TRAJ(r.pv, 2 * n * sizeof(float4));
     }
     return SF_OK;
 }
@@ -127,6 +127,7 @@ sf_status build_segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
         ds.nbr = r.nbr;
         ds.nbr_count = r.cnt;
         ds.sums = r.sums;
+        ds.pv = r.pv;
         if (ds.tune.list_mode == SF_LIST_NONE) ds.tune.list_mode = SF_LIST_TILE;
         sf::launch_density(ds, ctx->c, st);
         sf::launch_force_integrate(ds, ctx->c, st);
@@ -151,6 +152,7 @@ sf_status build_segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
         as.cnt = r.cnt;
         as.cs = r.cs;
         as.sums = r.sums;
+        as.pv = r.pv;
         sf::launch_adjoint_step(as, ctx->c, t->w, t->seg_partial + (size_t)s * nb, st);
     }
     sf::launch_adjoint_accumulate(t->seg_partial, len, n, t->w.scalars, st);

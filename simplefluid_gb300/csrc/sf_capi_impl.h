@@ -27,6 +27,7 @@ struct StepRec {
     uint32_t* cnt = nullptr;
     uint32_t* cs = nullptr;
     float4* sums = nullptr;
+    float4* pv = nullptr;  // 2n float4: the step's gather records
 };
 struct Trajectory {
     uint32_t nsteps = 0, ckpt = 0, n = 0, ncells_pad = 0;

@@ -183,13 +183,13 @@ struct AdjointStep {
     const uint32_t* cnt = nullptr;
     const uint32_t* cs = nullptr;
     const float4* sums = nullptr;
+    const float4* pv = nullptr;  // the step's 32-byte gather records (x, y, z, p), (vx, vy, vz, 1/rho)
 };
 // Adjoint working buffers (N particles).  Xb/Vb are indexed by particle id.
 struct AdjointWork {
     float4* Xb = nullptr;
     float4* Vb = nullptr;
-    float4* apb = nullptr;
-    float4* avb = nullptr;
+    float4* ab = nullptr;  // 2 per particle (32 bytes): apb = (cp tb, inv_bar), avb = (cv tb, cv_bar)
     float4* xdir = nullptr;
     float4* vdir = nullptr;
     float4* xf = nullptr;
