@@ -36,8 +36,13 @@ __device__ __forceinline__ void for_neighbours(const SimConst& c, uint32_t i, co
                                                F&& f) {
     const uint32_t m = __ldg(cnt + i);
     if (m <= (uint32_t)kNbCap) {
+        const uint32_t* lst = nbr + nbr_index(i, 0);  // slot k at lst[k * kNbTile]
+        uint32_t jn = __ldg(lst);
         for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t j = __ldg(nbr + nbr_index(i, k));
+            const uint32_t j = jn;
+            // the next index is in flight while this neighbour is processed
+            // (slots past the count hold stale values, never used)
+            jn = __ldg(lst + (size_t)min(k + 1, (uint32_t)kNbCap - 1) * kNbTile);
             if (j != i) f(j, ldg4(pos + j));  // the list records the particle itself
         }
     } else {
@@ -119,7 +124,8 @@ __device__ __forceinline__ void eos_derivs(const SimConst& c, float rho, float& 
 }
 
 // P2: force pair terms of every pair in both orientations, then the density
-// adjoint of the particle.  Outputs rhob, xf = (force x_bar, k_bar), vf.
+// adjoint of the particle.  Outputs xrb = (x, y, z, rho_bar), P4's gather
+// record, xf = (force x_bar, k_bar) and vf.
 // A neighbour is two 32-byte records, each one 256-bit load: the step's
 // (x, y, z, p | vx, vy, vz, 1/rho) and P1's (apb | avb).
 template <int kReach>
@@ -127,7 +133,7 @@ __global__ void __launch_bounds__(kAdjBlock)
     k_adj_forces(const float4* __restrict__ pos, const float4* __restrict__ pv, const float2* __restrict__ pr,
                  const float* __restrict__ rho, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
                  const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, const float4* __restrict__ ab,
-                 float* __restrict__ rhob, float4* __restrict__ xf, float4* __restrict__ vf) {
+                 float4* __restrict__ xrb, float4* __restrict__ xf, float4* __restrict__ vf) {
     const uint32_t k = blockIdx.x * kAdjBlock + threadIdx.x;
     if (k >= n) return;
     float4 xk, vk, apbk, avbk;
@@ -196,7 +202,7 @@ __global__ void __launch_bounds__(kAdjBlock)
     const float ib = apbk.w + invacc;
     float dpdrho, dpdk;
     eos_derivs(c, rho[k], dpdrho, dpdk);
-    rhob[k] = fmaf(pb, dpdrho, -((ib * invk) * invk));
+    xrb[k] = make_float4(xk.x, xk.y, xk.z, fmaf(pb, dpdrho, -((ib * invk) * invk)));
     xf[k] = make_float4(xb0, xb1, xb2, pb * dpdk);
     vf[k] = make_float4(vb0, vb1, vb2, 0.f);
 }
@@ -208,7 +214,7 @@ __global__ void __launch_bounds__(kAdjBlock)
 template <int kReach>
 __global__ void __launch_bounds__(kAdjBlock)
     k_adj_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
-                  const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, float m6cd, const float* __restrict__ rhob,
+                  const uint32_t* __restrict__ cnt, uint32_t n, SimConst c, float m6cd, const float4* __restrict__ xrb,
                   const float4* __restrict__ xdir, const float4* __restrict__ vdir, const float4* __restrict__ xf,
                   const float4* __restrict__ vf, const float4* __restrict__ ab, float4* __restrict__ Xb,
                   float4* __restrict__ Vb, double2* __restrict__ partial) {
@@ -227,13 +233,14 @@ __global__ void __launch_bounds__(kAdjBlock)
     if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(s0[0], s1[0]);
     if (k >= n) return;
     const float4 xk = pos[k];
-    const float rbk = rhob[k];
+    const float rbk = xrb[k].w;
     float x0 = 0.f, x1 = 0.f, x2 = 0.f;
-    for_neighbours<kReach>(c, k, xk, pos, cs, nbr, cnt, [&](uint32_t j, const float4& xj) {
+    for_neighbours<kReach>(c, k, xk, pos, cs, nbr, cnt, [&](uint32_t j, const float4&) {
+        const float4 xj = ldg4(xrb + j);  // position and rho_bar in one load
         const float d0 = xk.x - xj.x, d1 = xk.y - xj.y, d2 = xk.z - xj.z;
         const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
         const float q = c.h2 - r2;
-        const float sc = (rbk + __ldg(rhob + j)) * (q * q);
+        const float sc = (rbk + xj.w) * (q * q);
         x0 = fmaf(sc, d0, x0);
         x1 = fmaf(sc, d1, x1);
         x2 = fmaf(sc, d2, x2);
@@ -393,8 +400,8 @@ void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& 
     with_reach(c.reach, [&](auto R) {
         constexpr int K = decltype(R)::value;
         k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.pv, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.ab,
-                                                w.rhob, w.xf, w.vf);
-        k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.rhob, w.xdir, w.vdir,
+                                                w.xrb, w.xf, w.vf);
+        k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.xrb, w.xdir, w.vdir,
                                                  w.xf, w.vf, w.ab, w.Xb, w.Vb, partial);
     });
 }

@@ -170,7 +170,7 @@ void free_trajectory(sf_ctx* ctx) {
         if (p) cudaFree(p);
     for (auto& r : t->rec) free_rec(r);
     void* b[] = {t->snap, t->w.Xb, t->w.Vb, t->w.ab, t->w.xdir, t->w.vdir, t->w.xf, t->w.vf,
-                 t->w.rhob, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
+                 t->w.xrb, t->w.scalars, t->hist, t->e2, t->target, t->hpartial};
     for (void* p : b)
         if (p) cudaFree(p);
     delete t;

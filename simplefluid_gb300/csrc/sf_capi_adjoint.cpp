@@ -28,7 +28,7 @@ sf_status ensure_work(sf_ctx* ctx) {
     SF_ALLOC_TRAJ(w.vdir, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.xf, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.vf, n * sizeof(float4));
-    SF_ALLOC_TRAJ(w.rhob, n * sizeof(float));
+    SF_ALLOC_TRAJ(w.xrb, n * sizeof(float4));
     SF_ALLOC_TRAJ(w.scalars, 2 * sizeof(double));
     SF_ALLOC_TRAJ(t->snap, 2 * n * sizeof(float4));
     return SF_OK;

@@ -194,7 +194,7 @@ struct AdjointWork {
     float4* vdir = nullptr;
     float4* xf = nullptr;
     float4* vf = nullptr;
-    float* rhob = nullptr;
+    float4* xrb = nullptr;  // per particle (x, y, z, rho_bar): P4's gather record
     double* scalars = nullptr;   // [sum cv_bar, sum k_bar]
 };
 // One step's adjoint; its scalar block partials go to `partial`
