@@ -748,6 +748,14 @@ SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint3
     sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, pos_xyz ? io : nullptr, vel_xyz ? io + 3 * (size_t)n : nullptr,
                          ctx->stream);
     SF_TRY(check_launch("store state"));
+    if ((!pos_xyz || is_pinned(pos_xyz)) && (!vel_xyz || is_pinned(vel_xyz))) {
+        // page-locked outputs: both copies queued, one wait
+        if (pos_xyz) SF_CUDA(cudaMemcpyAsync(pos_xyz, io, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (vel_xyz)
+            SF_CUDA(cudaMemcpyAsync(vel_xyz, io + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
     if (pos_xyz) SF_TRY(copy_out(ctx, pos_xyz, io, bytes));
     if (vel_xyz) SF_TRY(copy_out(ctx, vel_xyz, io + 3 * (size_t)n, bytes));
     SF_CUDA(cudaStreamSynchronize(ctx->stream));
