@@ -1,0 +1,52 @@
+"""The bench's JSON line keeps its contract: the keys, their types and their
+consistency, for both arms (a short run of each)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(*args):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                         cwd=ROOT, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+def test_our_arm_line():
+    d = _run("--steps", "20", "--warmup", "3", "--cpu-seconds", "2", "--no-batched", "--no-adjoint",
+             "--no-other-workloads")
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks"):
+        assert k in d, k
+    assert d["n_gpus"] == 1 and d["steps"] == 20 and d["warmup"] == 3 and d["higher_is_better"] is True
+    assert d["unit"] == "particle-updates/s" and d["dtype"] == "f32" and d["scaling"] == "weak"
+    assert d["config"]["workload"] == "double_dambreak_1m" and d["config"]["particles"] == 1048576
+    n = d["config"]["particles"]
+    assert d["value"] == pytest.approx(n / (d["ms_per_step"] * 1e-3), rel=1e-6)
+    r = d["roofline"]
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+        assert k in r, k
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-9)
+    e = d["e2e"]
+    assert e["unit"] == d["unit"] and e["h2d_bytes_per_step"] == 2 * n * 12 and e["d2h_bytes_per_step"] == 2 * n * 12
+    assert 0 < e["value"] < d["value"] and e["state_finite"]
+    c = d["cpu_baseline"]
+    assert c["kind"] == "port" and c["cores"] >= 1 and c["value"] > 0
+    assert d["gpu_launches"] == 5 * d["steps"]
+    assert d["clocks"]["sm_max_mhz"] is None or d["clocks"]["sm_max_mhz"] > 0
+
+
+def test_reference_arm_line():
+    d = _run("--impl", "reference", "--steps", "3", "--warmup", "3")
+    assert d["impl"] == "reference" and d["unit"] == "particle-updates/s" and d["value"] > 0
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
