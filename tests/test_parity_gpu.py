@@ -398,3 +398,37 @@ def test_full_size_sphere_pool(oracle):
     assert np.isfinite(gpos).all() and np.isfinite(gvel).all()
     lo, hi = np.float32(0.00227), np.float32(1 - 0.00227)
     assert np.all(gpos >= lo) and np.all(gpos <= hi)
+
+
+def test_large_scale_16m_lattice(oracle):
+    """16,000,000 particles (a 200 x 400 x 200 jittered lattice, 72M grid
+    cells): after 5 steps the state checks are clean (sorted, permutation,
+    cell table, inside the box, finite), and the densities of 200 sampled
+    particles equal all-pairs sums over their kd-tree neighbourhoods (FP64,
+    within the FP32 summation-order band)."""
+    spatial = pytest.importorskip("scipy.spatial")
+    r = 0.0012
+    prm = params_16k(particleRadius=r, kernelRadius=4 * r)
+    rng = np.random.default_rng(16)
+    g = np.stack(np.meshgrid(np.arange(200), np.arange(400), np.arange(200), indexing="ij"), -1).reshape(-1, 3)
+    pos = (0.01 + 2 * r * g + rng.uniform(-0.2, 0.2, size=g.shape) * 2 * r).astype(np.float32)
+    del g
+    n = pos.shape[0]
+    assert n == 16_000_000
+    with solver_with(prm, pos) as s:
+        s.makeReady()
+        s.step(5)
+        rep = s.checkState()
+        assert all(rep[k] == 0 for k in ("non_finite", "outside_box", "unsorted", "cell_table_mismatch", "bad_ids"))
+        assert rep["n"] == n
+        rho, _ = s.computeDensity()
+        spos, _, ids, _ = s.sortedState()
+    h = np.float64(np.float32(4 * r))
+    d = oracle.derive(prm.to_c())
+    tree = spatial.cKDTree(spos.astype(np.float64))
+    sample = rng.choice(n, 200, replace=False)
+    for i in sample:
+        nb = tree.query_ball_point(spos[i].astype(np.float64), float(h))
+        r2 = ((spos[nb].astype(np.float64) - spos[i].astype(np.float64)) ** 2).sum(1)
+        w = ((h * h - r2[r2 < h * h]) ** 3).sum()
+        assert abs(rho[i] / (d["cd"] * w) - 1.0) < 2e-5
