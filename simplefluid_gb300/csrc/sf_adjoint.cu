@@ -143,10 +143,7 @@ __global__ void __launch_bounds__(kAdjBlock)
     const float pk = prk.x, invk = prk.y;
     float pb = 0.f, invacc = 0.f;
     float xb0 = 0.f, xb1 = 0.f, xb2 = 0.f, vb0 = 0.f, vb1 = 0.f, vb2 = 0.f;
-    for_neighbours<kReach>(c, k, pos[k], pos, cs, nbr, cnt, [&](uint32_t j, const float4&) {
-        float4 xj, vj, apbj, avbj;
-        ld8(pv + 2 * (size_t)j, xj, vj);
-        ld8(ab + 2 * (size_t)j, apbj, avbj);
+    auto pair = [&](const float4& xj, const float4& vj, const float4& apbj, const float4& avbj) {
         const float d0 = xk.x - xj.x, d1 = xk.y - xj.y, d2 = xk.z - xj.z;
         const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
         const float r = sqrtf(r2);
@@ -198,7 +195,41 @@ __global__ void __launch_bounds__(kAdjBlock)
             xb1 = fmaf(g, d1, xb1);
             xb2 = fmaf(g, d2, xb2);
         }
-    });
+    };
+    const uint32_t m = __ldg(cnt + k);
+    if (m <= (uint32_t)kNbCap) {
+        // The next neighbour's records and the index after it are in flight
+        // while a neighbour is processed.  The list holds the particle itself
+        // (skipped); slots past the count hold stale values, never used.
+        const uint32_t* lst = nbr + nbr_index(k, 0);  // slot s at lst[s * kNbTile]
+        uint32_t jc = __ldg(lst), jn = __ldg(lst + kNbTile);
+        float4 nx, nv, na, nb;
+        if (m) {
+            ld8(pv + 2 * (size_t)jc, nx, nv);
+            ld8(ab + 2 * (size_t)jc, na, nb);
+        }
+        for (uint32_t s = 0; s < m; ++s) {
+            const uint32_t j = jc;
+            const float4 xj = nx, vj = nv, apbj = na, avbj = nb;
+            if (s + 1 < m) {
+                jc = jn;
+                jn = __ldg(lst + (size_t)min(s + 2, (uint32_t)kNbCap - 1) * kNbTile);
+                ld8(pv + 2 * (size_t)jc, nx, nv);
+                ld8(ab + 2 * (size_t)jc, na, nb);
+            }
+            if (j != k) pair(xj, vj, apbj, avbj);
+        }
+    } else {
+        for_candidates<kReach>(c, cs, pos, xk.x, xk.y, xk.z, [&](uint32_t j, const float4& xp) {
+            if (j == k) return;
+            const float dx = xk.x - xp.x, dy = xk.y - xp.y, dz = xk.z - xp.z;
+            if (!(fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)) return;
+            float4 xj, vj, apbj, avbj;
+            ld8(pv + 2 * (size_t)j, xj, vj);
+            ld8(ab + 2 * (size_t)j, apbj, avbj);
+            pair(xj, vj, apbj, avbj);
+        });
+    }
     const float ib = apbk.w + invacc;
     float dpdrho, dpdk;
     eos_derivs(c, rho[k], dpdrho, dpdk);
