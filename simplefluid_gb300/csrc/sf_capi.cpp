@@ -374,6 +374,20 @@ sf_status copy_in(sf_ctx* ctx, void* dst, const void* src, size_t bytes) {
     return SF_OK;
 }
 
+// Fewer than this many particles fill few warps per SM: each force-pass thread
+// then keeps four neighbours in flight instead of two (measured 5-6% faster
+// steps at 16k-64k particles; two are faster at 1M).
+constexpr uint32_t kSmallScene = 262144;
+
+void apply_size_defaults(sf_ctx* ctx) {
+    if (ctx->tune_explicit || ctx->d.table) return;  // batches use prefetch 2
+    const int pf = ctx->d.n < kSmallScene ? 4 : 2;
+    if (ctx->d.tune.prefetch != pf) {
+        ctx->d.tune.prefetch = pf;
+        drop_graph(ctx);
+    }
+}
+
 // Every resource a context owns (also the engine embedded in a batch).
 void release_ctx(sf_ctx* ctx) {
     cudaSetDevice(ctx->device);
@@ -709,6 +723,7 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
     if (resized) drop_graph(ctx);
     ctx->d.n = n;
     ctx->sorted = false;
+    apply_size_defaults(ctx);
     if (n == 0) return SF_OK;
     if (vel_xyz && is_pinned(pos_xyz) && is_pinned(vel_xyz)) {
         SF_TRY(upload_overlapped(ctx, pos_xyz, vel_xyz));
@@ -810,6 +825,7 @@ SF_API sf_status sf_set_state_device(sf_ctx* ctx, const float* d_pos_xyz, const 
     if (resized) drop_graph(ctx);
     ctx->d.n = n;
     ctx->sorted = false;
+    apply_size_defaults(ctx);
     if (n == 0) return SF_OK;
     SF_TRY(stream_after(ctx->stream, (cudaStream_t)other));
     return sort_uploaded(ctx, d_pos_xyz, d_vel_xyz);

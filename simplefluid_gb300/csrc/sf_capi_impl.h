@@ -64,6 +64,7 @@ struct sf_ctx {
     // tables (Grace: NVLink-C2C with address translation): -1 unknown, 0, 1
     int host_direct = -1;
     uint32_t* d_report = nullptr;  // sf_check_state counters
+    bool tune_explicit = false;    // sf_set_tuning was called: keep its choices
     cudaGraphExec_t step_graph = nullptr;
     bool sorted = false;  // particles uploaded and cell-sorted
     float* h_stage = nullptr;  // pinned staging for pageable caller buffers
@@ -151,6 +152,8 @@ sf_status upload_overlapped(sf_ctx* ctx, const float* pos_xyz, const float* vel_
 void enqueue_full_step(sf_ctx* ctx);
 sf_status capture_step(sf_ctx* ctx);
 void drop_graph(sf_ctx* ctx);
+// Kernel choices by particle count, unless the caller set them explicitly.
+void apply_size_defaults(sf_ctx* ctx);
 
 #define SF_CUDA(call)                                      \
     do {                                                   \

@@ -208,6 +208,7 @@ SF_API sf_status sf_set_tuning(sf_ctx* ctx, const sf_tuning* t) {
     ctx->d.tune.density_block = t->density_block;
     ctx->d.tune.force_block = t->force_block;
     ctx->d.tune.prefetch = t->prefetch;
+    ctx->tune_explicit = true;
     drop_graph(ctx);
     return SF_OK;
 }
@@ -409,6 +410,7 @@ SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_o
     if (resized) drop_graph(ctx);
     ctx->d.n = n;
     ctx->sorted = false;
+    apply_size_defaults(ctx);
     if (n) {
         sf::DeviceState& d = ctx->d;
         SF_TRY(copy_in(ctx, d.io, pv.data(), pv.size() * sizeof(float)));

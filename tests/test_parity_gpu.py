@@ -432,3 +432,28 @@ def test_large_scale_16m_lattice(oracle):
         r2 = ((spos[nb].astype(np.float64) - spos[i].astype(np.float64)) ** 2).sum(1)
         w = ((h * h - r2[r2 < h * h]) ** 3).sum()
         assert abs(rho[i] / (d["cd"] * w) - 1.0) < 2e-5
+
+
+def test_gather_depth_follows_scene_size_unless_set():
+    """Small scenes gather four neighbours per batch, large ones two; an
+    explicit sf_set_tuning is kept across uploads."""
+    import ctypes
+    lib = C.load()
+
+    def prefetch(s):
+        t = C.sf_tuning()
+        C.check(lib.sf_get_tuning(s.handle, ctypes.byref(t)))
+        return t.prefetch
+
+    prm = params_16k()
+    small = jittered_block()
+    big = np.concatenate([jittered_block(n_side=(64, 64, 64), spacing=0.0125, seed=s, origin=0.05 + 0.1 * s)
+                          for s in range(2)])
+    assert small.shape[0] < 262144 <= big.shape[0]
+    with solver_with(prm, small) as s:
+        assert prefetch(s) == 4
+        s.setParticles(big)
+        assert prefetch(s) == 2
+        C.check(lib.sf_set_tuning(s.handle, ctypes.byref(C.sf_tuning(2, 128, 128, 2))))
+        s.setParticles(small)
+        assert prefetch(s) == 2
