@@ -184,6 +184,16 @@ public:
     }
 
     void synchronize() { check(sf_synchronize(m_Ctx)); }
+
+    // Invariants of the device state (sf_check_state): non-finite values,
+    // particles outside the box, sort and particle-index consistency.
+    sf_state_report checkState() {
+        upload_if_dirty();
+        sf_state_report r{};
+        check(sf_check_state(m_Ctx, &r));
+        return r;
+    }
+
     sf_ctx* handle() { return m_Ctx; }
     const std::shared_ptr<SPHParameters<float>>& params() const { return m_Params; }
 

@@ -40,6 +40,13 @@ int main(int argc, char** argv) {
         out.write(reinterpret_cast<const char*>(pos.data()), n * sizeof(simplefluid::Vec3f));
         out.write(reinterpret_cast<const char*>(vel.data()), n * sizeof(simplefluid::Vec3f));
         std::printf("particles=%u substeps=%d frames=%d simtime=%.6f\n", nparticles, substeps, nframes, sim.simTime());
+        // a healthy state after the run
+        const sf_state_report rep = sim.solver().checkState();
+        if (rep.n != n || rep.non_finite || rep.outside_box || rep.unsorted || rep.cell_table_mismatch ||
+            rep.bad_ids) {
+            std::fprintf(stderr, "state check failed\n");
+            return 1;
+        }
         // the same frames with no per-sub-step observer run on the device
         {
             simplefluid::Simulator sim2;
