@@ -311,8 +311,7 @@ sf_status upload_overlapped(sf_ctx* ctx, const float* pos_xyz, const float* vel_
 void enqueue_full_step(sf_ctx* ctx) {
     if (ctx->c.adaptive) {
         sf::DeviceState dr = ctx->d;
-        dr.frame = ctx->frame;
-        sf::launch_choose_dt(ctx->frame, ctx->c, ctx->stream);
+        dr.frame = ctx->frame;  // the density pass chooses dt, the force pass reads it
         sf::enqueue_step(dr, ctx->c, ctx->stream);
     } else {
         sf::enqueue_step(ctx->d, ctx->c, ctx->stream);
@@ -909,8 +908,7 @@ static sf_status build_frame_graph(sf_ctx* ctx, double frame_time, uint32_t max_
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     SF_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     sf::DeviceState dr = ctx->d;
-    dr.frame = ctx->frame;
-    sf::launch_choose_dt(ctx->frame, ctx->c, ctx->stream);
+    dr.frame = ctx->frame;  // the density pass chooses dt, the force pass reads it
     sf::enqueue_step(dr, ctx->c, ctx->stream);
     sf::launch_frame_check(ctx->frame, frame_time, max_substeps, h, ctx->stream);
     SF_CUDA(cudaStreamEndCapture(ctx->stream, &body));

@@ -25,10 +25,13 @@ __global__ void __launch_bounds__(kBlockSize)
     k_density(const float4* __restrict__ pos, const uint32_t* __restrict__ cs, uint32_t n, SimConst c0,
               const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
               float* __restrict__ rho_out, float2* __restrict__ pr_out, uint32_t* __restrict__ nbr,
-              uint32_t* __restrict__ nbr_count, const float4* __restrict__ vel, float4* __restrict__ pv) {
+              uint32_t* __restrict__ nbr_count, const float4* __restrict__ vel, float4* __restrict__ pv,
+              FrameState* __restrict__ frame) {
     __shared__ uint32_t s_nb[kMode == kEmitStaged ? kNbCap : 1][kMode == kEmitStaged ? kBlockSize : 1];
     grid_dependency_wait();
     allow_dependents();
+    // a stepping pass with a frame state chooses this sub-step's dt
+    if (frame && blockIdx.x == 0 && threadIdx.x == 0) choose_dt(frame, c0);
     const uint32_t t = threadIdx.x;
     const uint32_t i = blockIdx.x * kBlockSize + t;
     uint32_t cnt = 0;
@@ -76,10 +79,11 @@ void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
             if constexpr (K <= 2)
                 launch_chained(k_density<kMode, kBlockSize, K, true>, grid_for(d.n, kBlockSize), kBlockSize, s,
                                d.pos, d.cell_start, d.n, c, d.table, d.scene_off, d.nscenes, d.rho, d.pr, d.nbr,
-                               d.nbr_count, d.vel, d.pv);
+                               d.nbr_count, d.vel, d.pv, (FrameState*)nullptr);
         } else {
             launch_chained(k_density<kMode, kBlockSize, K, false>, grid_for(d.n, kBlockSize), kBlockSize, s, d.pos,
-                           d.cell_start, d.n, c, nullptr, nullptr, 0u, d.rho, d.pr, d.nbr, d.nbr_count, d.vel, d.pv);
+                           d.cell_start, d.n, c, nullptr, nullptr, 0u, d.rho, d.pr, d.nbr, d.nbr_count, d.vel, d.pv,
+                           d.frame);
         }
     });
 }

@@ -248,6 +248,20 @@ __device__ __forceinline__ void st8(float4* __restrict__ p, const float4& a, con
                  : "memory");
 }
 
+// The sub-step's dt from the previous sub-step's maxima (adaptive: CFL on
+// |v| and |a|; fixed: time_step), then the maxima restart for this sub-step.
+__device__ __forceinline__ void choose_dt(FrameState* __restrict__ fs, const SimConst& c) {
+    float dt = c.dt;
+    if (c.adaptive) {
+        const float v2 = __uint_as_float(fs->v2max_bits), a2 = __uint_as_float(fs->a2max_bits);
+        if (v2 > 0.f) dt = fminf(dt, (c.cfl_v * c.h) / sqrtf(v2));
+        if (a2 > 0.f) dt = fminf(dt, c.cfl_a * sqrtf(c.h / sqrtf(a2)));
+    }
+    fs->dt = dt;
+    fs->v2max_bits = 0u;
+    fs->a2max_bits = 0u;
+}
+
 // Equation of state and the p >= 0 clamp (SPHParameters::bUseAttractivePressure).
 __device__ __forceinline__ float pressure_of(const SimConst& c, float rho) {
     float p;

@@ -5,27 +5,13 @@
 //
 // Adaptive sub-step: dt = min(time_step, 0.4 h / max|v|, 0.25 sqrt(h / max|a|))
 // with both maxima taken over the previous sub-step (|v| after integration),
-// which keeps forces and integration in one fused pass.  The CPU oracle
-// restates the same rule.
+// which keeps forces and integration in one fused pass.  The density pass's
+// first thread chooses dt (choose_dt in sf_device.cuh) before the force pass
+// reads it.  The CPU oracle restates the same rule.
 #include "sf_device.cuh"
 
 namespace sf {
 namespace {
-
-__global__ void k_choose_dt(FrameState* __restrict__ fs, SimConst c) {
-    grid_dependency_wait();
-    allow_dependents();
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    float dt = c.dt;
-    if (c.adaptive) {
-        const float v2 = __uint_as_float(fs->v2max_bits), a2 = __uint_as_float(fs->a2max_bits);
-        if (v2 > 0.f) dt = fminf(dt, (c.cfl_v * c.h) / sqrtf(v2));
-        if (a2 > 0.f) dt = fminf(dt, c.cfl_a * sqrtf(c.h / sqrtf(a2)));
-    }
-    fs->dt = dt;
-    fs->v2max_bits = 0u;
-    fs->a2max_bits = 0u;
-}
 
 // max |v|^2 of the state (non-negative floats order like their bits): one
 // atomic per block of kMaxBlock threads.
@@ -69,8 +55,6 @@ __global__ void k_frame_check(FrameState* __restrict__ fs, double frame_time, ui
 }
 
 }  // namespace
-
-void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s) { launch_chained(k_choose_dt, 1, 32, s, fs, c); }
 
 void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s) {
     cudaMemsetAsync(&fs->v2max_bits, 0, 2 * sizeof(uint32_t), s);

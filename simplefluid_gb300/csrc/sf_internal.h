@@ -162,7 +162,6 @@ void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream
 
 // ---- sub-step control (sf_frame.cu) ------------------------------------
 // dt of the next sub-step from the maxima (adaptive) or the fixed step; clears the maxima.
-void launch_choose_dt(FrameState* fs, const SimConst& c, cudaStream_t s);
 // Maxima of the uploaded state: |v|^2 over the particles, |a|^2 = 0.
 void launch_init_maxima(const float4* vel, uint32_t n, FrameState* fs, cudaStream_t s);
 void launch_frame_begin(FrameState* fs, cudaStream_t s);
