@@ -39,17 +39,21 @@ __global__ void __launch_bounds__(kBlockSize)
         const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
         const float4 xi = pos[i];
         float s = 0.f;
+        uint32_t* const lst = kMode == kEmitTile ? nbr + nbr_index(i, 0) : nullptr;  // slot k at lst[k * kNbTile]
         for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             const bool near = r2 < c.h2;
             const float q = near ? c.h2 - r2 : 0.f;
             s = fmaf(q * q, q, s);
-            if (kMode != kEmitNone && near) {
-                if (cnt < kNbCap) {
-                    if (kMode == kEmitStaged) s_nb[cnt][t] = j;
-                    if (kMode == kEmitTile) nbr[nbr_index(i, cnt)] = j;
-                }
+            if (kMode == kEmitTile) {
+                // Predicated store, no branch.  Past the cap the last slot is
+                // overwritten: such a list is never read (the force pass
+                // rescans particles whose count exceeds the cap).
+                store_if(lst + (size_t)min(cnt, (uint32_t)kNbCap - 1) * kNbTile, j, near);
+                cnt += near ? 1u : 0u;
+            } else if (kMode == kEmitStaged && near) {
+                if (cnt < kNbCap) s_nb[cnt][t] = j;
                 ++cnt;
             }
         });

@@ -197,6 +197,13 @@ __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t
     });
 }
 
+// *p = v where `pred` holds, as one predicated store (no branch).  No memory
+// clobber: the caller's kernel never reads what these stores write.
+__device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool pred) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u32 [%0], %1;\n\t}" ::"l"(p),
+                 "r"(v), "r"((uint32_t)pred));
+}
+
 // The candidate walk above with both row loops rolled and the gaps computed
 // per row.
 template <int kReach, typename F>
