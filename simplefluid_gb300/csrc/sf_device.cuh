@@ -292,8 +292,7 @@ __device__ __forceinline__ size_t nbr_index(uint32_t i, uint32_t k) {
 }
 
 // Pair terms of particle i with neighbour j (|xi - xj| < h; j == i adds exact
-// zeros), in the
-// oracle's operation order.
+// zeros), in the oracle's operation order.
 struct PairAcc {
     float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
 };
@@ -308,12 +307,16 @@ __device__ __forceinline__ void pair_terms(const SimConst& c, const float4& xi, 
     a.avx = fmaf(w, vj.x - vi.x, a.avx);
     a.avy = fmaf(w, vj.y - vi.y, a.avy);
     a.avz = fmaf(w, vj.z - vi.z, a.avz);
-    if (r > 0.f) {
-        const float sp = ((pi + prj.x) * w) * (hr / r);
-        a.apx = fmaf(sp, dx, a.apx);
-        a.apy = fmaf(sp, dy, a.apy);
-        a.apz = fmaf(sp, dz, a.apz);
-    }
+    // The pressure term needs r > 0.  Without a branch: the quotient is taken
+    // over r = 1 where r == 0 (so it stays finite), then the term's weight is
+    // set to zero there, and fma(0, d, a) == a (d is finite, and an
+    // accumulator that starts at +0 is never -0).
+    const bool apart = r > 0.f;
+    const float sp_r = ((pi + prj.x) * w) * (hr / (apart ? r : 1.f));
+    const float sp = apart ? sp_r : 0.f;
+    a.apx = fmaf(sp, dx, a.apx);
+    a.apy = fmaf(sp, dy, a.apy);
+    a.apz = fmaf(sp, dz, a.apz);
 }
 
 }  // namespace sf
