@@ -55,12 +55,14 @@ __device__ __forceinline__ void force_one(
             for (int u = 0; u < kPrefetch; ++u)
                 pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
         }
-        for (; k < cnt; ++k) {
-            const uint32_t j = __ldg(nbr + nbr_index(i, k));
-            float4 xj, vj;
-            ld8(pv + 2 * (size_t)j, xj, vj);
-            pair_terms(c, xi, vi, pri.x, xj, make_float2(xj.w, vj.w), vj, a);
-        }
+        // the last cnt - k < kPrefetch neighbours: their indices are in jn
+        float4 xj[kPrefetch - 1], vj[kPrefetch - 1];
+#pragma unroll
+        for (int u = 0; u < kPrefetch - 1; ++u)
+            if (k + u < cnt) ld8(pv + 2 * (size_t)jn[u], xj[u], vj[u]);
+#pragma unroll
+        for (int u = 0; u < kPrefetch - 1; ++u)
+            if (k + u < cnt) pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
     } else {
         for_candidates_rolled<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             if (j == i) return;
