@@ -6,6 +6,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "sf_internal.h"
@@ -15,6 +17,19 @@ namespace sf {
 constexpr int kBlock = 256;
 
 inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// Streaming multiprocessors of the current device (queried once per device).
+inline int sm_count() {
+    constexpr int kDevices = 64;
+    static std::atomic<int> cached[kDevices] = {};
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < kDevices && (v = cached[dev].load(std::memory_order_relaxed)) > 0) return v;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    v = std::max(v, 1);
+    if (dev >= 0 && dev < kDevices) cached[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 
 // Programmatic dependent launch.  The kernels of a sub-step are launched with
 // launch_chained(): each may begin launching while its predecessor in the

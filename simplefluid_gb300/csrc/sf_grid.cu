@@ -180,37 +180,53 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_totals(const uint4* __res
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
-// Exclusive scan of the cell histogram into the cell table.  Block b scans
-// tile b (kScanTile cells) and adds the totals of tiles 0..b-1, which the
-// histogram atomics accumulated in tile_sums, so one kernel does the whole scan.
-// The predecessor sum and the tile's scan share one two-barrier pass.
-__global__ void __launch_bounds__(kScanThreads) k_scan(const uint4* __restrict__ counts,
-                                                       const uint32_t* __restrict__ tile_sums,
-                                                       uint4* __restrict__ cell_start) {
+// Exclusive scan of the cell histogram into the cell table, in one kernel.
+// Block b scans the contiguous scan tiles [t0, t1) (kScanTile cells each; a
+// few blocks per SM): it sums the totals of the tiles before t0 once (the
+// histogram atomics accumulated them in tile_sums), then carries the running
+// offset from tile to tile, loading the next tile's counts while it scans the
+// current one.  Two barriers per tile; the warp totals alternate between two
+// shared buffers so that a tile's writes never meet the previous tile's reads.
+__global__ void __launch_bounds__(kScanThreads, kScanBlocksPerSM) k_scan(const uint4* __restrict__ counts,
+                                                                         const uint32_t* __restrict__ tile_sums,
+                                                                         uint32_t ntiles,
+                                                                         uint4* __restrict__ cell_start) {
     static_assert(kScanThreads == 1024, "one warp-sum slot per warp");
     grid_dependency_wait();
     allow_dependents();
-    __shared__ uint32_t s_warp[32], s_before[32];
+    __shared__ uint32_t s_warp[2][32], s_before[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t t = (size_t)blockIdx.x * kScanThreads + threadIdx.x;
-    const uint4 q = counts[t];
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = blockIdx.x * per, t1 = min(t0 + per, ntiles);
+    if (t0 >= t1) return;  // the whole block
+    uint4 q = counts[(size_t)t0 * kScanThreads + threadIdx.x];
     uint32_t before = 0;
-    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += kScanThreads) before += tile_sums[k];
-    const uint32_t v = q.x + q.y + q.z + q.w;
-    const uint32_t inc = warp_inclusive(v);
+    for (uint32_t k = threadIdx.x; k < t0; k += kScanThreads) before += tile_sums[k];
     before = __reduce_add_sync(0xffffffffu, before);
-    if (lane == 31) s_warp[warp] = inc;
     if (lane == 0) s_before[warp] = before;
     __syncthreads();
-    if (warp == 0) {
-        const uint32_t w = s_warp[lane];
-        const uint32_t wi = warp_inclusive(w);
-        const uint32_t b = __reduce_add_sync(0xffffffffu, s_before[lane]);
-        s_warp[lane] = wi - w + b;  // cells of the earlier warps and tiles
+    // warp 0 carries the offset of the current tile (the same in every lane)
+    uint32_t base = warp == 0 ? __reduce_add_sync(0xffffffffu, s_before[lane]) : 0u;
+    for (uint32_t t = t0; t < t1; ++t) {
+        uint32_t* const ws = s_warp[(t - t0) & 1];
+        uint4 qn = make_uint4(0u, 0u, 0u, 0u);
+        if (t + 1 < t1) qn = counts[(size_t)(t + 1) * kScanThreads + threadIdx.x];
+        const uint32_t v = q.x + q.y + q.z + q.w;
+        const uint32_t inc = warp_inclusive(v);
+        if (lane == 31) ws[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = ws[lane];
+            const uint32_t wi = warp_inclusive(w);
+            ws[lane] = wi - w + base;  // cells of the earlier warps and tiles
+            base += __shfl_sync(0xffffffffu, wi, 31);
+        }
+        __syncthreads();
+        const uint32_t ex = ws[warp] + inc - v;
+        cell_start[(size_t)t * kScanThreads + threadIdx.x] =
+            make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
+        q = qn;
     }
-    __syncthreads();
-    const uint32_t ex = s_warp[warp] + inc - v;
-    cell_start[t] = make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
 }
 
 // ---------------------------------------------------------------- reorder
@@ -386,7 +402,8 @@ void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimC
 }
 
 void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
-    launch_chained(k_scan, d.ntiles, kScanThreads, s, reinterpret_cast<const uint4*>(d.counts), d.tile_sums,
+    const uint32_t blocks = std::min<uint32_t>(d.ntiles, (uint32_t)(kScanBlocksPerSM * sm_count()));
+    launch_chained(k_scan, blocks, kScanThreads, s, reinterpret_cast<const uint4*>(d.counts), d.tile_sums, d.ntiles,
                    reinterpret_cast<uint4*>(d.cell_start));
 }
 

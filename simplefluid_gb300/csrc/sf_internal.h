@@ -110,6 +110,7 @@ constexpr int kEmitNone = 0, kEmitStaged = 1, kEmitTile = 2;
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kScanBlocksPerSM = 2;  // resident scan blocks per SM (the scan grid's size)
 
 // ---- kernel launchers (sf_grid.cu, sf_density.cu, sf_force.cu); all enqueue on `s`
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
