@@ -28,6 +28,7 @@ __device__ __forceinline__ void force_one(
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint32_t* __restrict__ counts,
     uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
     float4* __restrict__ sums, const FrameState* __restrict__ frame, uint32_t& v2, uint32_t& a2) {
+    static_assert(kPrefetch >= 2, "the list tail holds up to kPrefetch - 1 neighbours");
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 xi = pos[i];
     const float4 vi = vel[i];
