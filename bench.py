@@ -29,6 +29,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -139,6 +140,29 @@ def make_params(workload: str):
     return SPHParameters(particleRadius=w["particleRadius"], kernelRadius=w["kernelRadius"], scene=w["scene"],
                          pressureStiffness=50.0, viscosity=0.01, restDensity=1000.0, timeStep=1e-4,
                          boundaryRestitution=0.1)
+
+
+def host_cpu() -> dict:
+    """The host the CPU baselines ran on: architecture, CPU model and logical CPUs."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith("model name"):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"machine": platform.machine(), "cpu_model": model, "logical_cpus": os.cpu_count()}
 
 
 def cpu_oracle_rate(pos: np.ndarray, prm, budget_s: float, max_steps: int, warmup: int = 1):
@@ -417,7 +441,8 @@ def run_reference(args, workload):
         "config": {"workload": workload, "particles": int(pos.shape[0]), "kernel_radius": prm.kernelRadius,
                    "particle_radius": prm.particleRadius, "dt": prm.timeStep},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
-                         "note": "CPU restatement (reference TBB solver library unavailable: not in the reference tree)"},
+                         "note": "CPU restatement (reference TBB solver library unavailable: not in the reference tree)",
+                         "host": host_cpu()},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -530,7 +555,8 @@ def run_ours(args, workload):
         rate, steps, threads = cpu_oracle_rate(pos, prm, args.cpu_seconds, 200)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{steps} sub-steps of the {n}-particle {workload} from its initial state (after 1 warm-up), "
-                         f"CPU oracle with {threads} OpenMP threads; reference TBB solver library unavailable"}
+                         f"CPU oracle with {threads} OpenMP threads; reference TBB solver library unavailable",
+               "host": host_cpu()}
 
     solver.close()
     batched = measure_batched(args, dist, rank, ws) if not args.no_batched else None
