@@ -244,6 +244,29 @@ def test_edge_dense_cluster_one_cell(oracle):
     assert normwise_err(gpos, opos) < 1e-5
 
 
+def test_edge_coincident_pairs_on_the_list_path(oracle):
+    """Coincident distinct particles (r = 0, j != i) with short neighbour lists:
+    the force pass's list path takes no pressure term for them, like the
+    oracle, and the trajectory stays bit-identical."""
+    prm = params_16k()
+    pos = jittered_block(n_side=(10, 12, 10), seed=21)
+    pos[[5, 117, 640, 999]] = pos[[6, 118, 641, 1000]]
+    vel = np.random.default_rng(22).normal(scale=0.05, size=pos.shape).astype(np.float32)
+    vel[[5, 117, 640, 999]] = vel[[6, 118, 641, 1000]]
+    with solver_with(prm, pos, vel) as s:
+        s.step(30)
+        gpos, gvel = s.getState()
+        rep = s.checkState()
+    assert rep["list_overflow"] == 0 and rep["non_finite"] == 0  # the lists were read, not rescanned
+    st = oracle.State(pos, vel)
+    st.step(prm.to_c(), 30)
+    st.sort(prm.to_c())
+    opos, ovel = st.original_order()
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32))
+    assert np.array_equal(gpos[5], gpos[6]) and np.array_equal(gpos[999], gpos[1000])
+
+
 def test_edge_particles_outside_box(oracle):
     """Particles given outside the box are binned into the edge cells and
     clamped back by the first step."""
