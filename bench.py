@@ -618,10 +618,14 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-other-workloads", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--only", choices=["adjoint"], default=None,
+                    help="run one section alone and print its record (for profiling); not the bench line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.only == "adjoint":
+        print(json.dumps({"section": "adjoint", **measure_adjoint(args)}), flush=True)
+    elif args.impl == "reference":
         run_reference(args, args.workload)
     else:
         run_ours(args, args.workload)

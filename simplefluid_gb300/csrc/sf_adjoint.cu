@@ -282,41 +282,47 @@ __global__ void __launch_bounds__(kAdjBlock)
     Vb[id] = make_float4(vd.x + vfk.x, vd.y + vfk.y, vd.z + vfk.z, 0.f);
 }
 
-// Adds the block partials of `nsteps` steps to acc[0..1]: per step, thread t
-// sums blocks t, t + 256, ... in order, a fixed shared-memory tree combines
-// the threads, and the step sums are added last step first (the order the
-// adjoint visits them).  Deterministic.
+// Adds the block partials of `nsteps` steps to acc[0..1].  Eight steps at a
+// time, one warp per step: lane l sums blocks l, l + 32, ... in order and a
+// fixed shuffle tree combines the lanes; thread 0 then adds the step sums
+// last step first (the order the adjoint visits them).  Deterministic.
 constexpr int kAccThreads = 256;
 
 __global__ void __launch_bounds__(kAccThreads)
     k_accumulate_scalars(const double2* __restrict__ partial, uint32_t nsteps, uint32_t nblocks,
                          double* __restrict__ acc) {
-    __shared__ double s0[kAccThreads], s1[kAccThreads];
+    constexpr int kWarps = kAccThreads / 32;
+    __shared__ double s0[kWarps], s1[kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double a = 0.0, b = 0.0;
     if (threadIdx.x == 0) {
         a = acc[0];
         b = acc[1];
     }
-    for (int64_t st = (int64_t)nsteps - 1; st >= 0; --st) {
+    for (int64_t hi = (int64_t)nsteps; hi > 0; hi -= kWarps) {
+        const int64_t st = hi - 1 - warp;  // the same in every lane of the warp
         double x = 0.0, y = 0.0;
-        for (uint32_t t = threadIdx.x; t < nblocks; t += kAccThreads) {
-            const double2 v = partial[(size_t)st * nblocks + t];
-            x += v.x;
-            y += v.y;
-        }
-        s0[threadIdx.x] = x;
-        s1[threadIdx.x] = y;
-        __syncthreads();
-        for (int o = kAccThreads / 2; o > 0; o >>= 1) {
-            if ((int)threadIdx.x < o) {
-                s0[threadIdx.x] += s0[threadIdx.x + o];
-                s1[threadIdx.x] += s1[threadIdx.x + o];
+        if (st >= 0) {
+            for (uint32_t t = lane; t < nblocks; t += 32) {
+                const double2 v = partial[(size_t)st * nblocks + t];
+                x += v.x;
+                y += v.y;
             }
-            __syncthreads();
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_down_sync(0xffffffffu, x, o);
+                y += __shfl_down_sync(0xffffffffu, y, o);
+            }
         }
+        if (lane == 0) {
+            s0[warp] = x;
+            s1[warp] = y;
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
-            a += s0[0];
-            b += s1[0];
+            for (int w = 0; w < kWarps && hi - 1 - w >= 0; ++w) {  // steps hi-1, hi-2, ...
+                a += s0[w];
+                b += s1[w];
+            }
         }
         __syncthreads();
     }
