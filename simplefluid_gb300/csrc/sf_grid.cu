@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_totals(const uint4* __res
 // shared buffers so that a tile's writes never meet the previous tile's reads.
 __global__ void __launch_bounds__(kScanThreads, kScanBlocksPerSM) k_scan(const uint4* __restrict__ counts,
                                                                          const uint32_t* __restrict__ tile_sums,
-                                                                         uint32_t ntiles,
+                                                                         uint32_t ntiles, uint32_t n,
                                                                          uint4* __restrict__ cell_start) {
     static_assert(kScanThreads == 1024, "one warp-sum slot per warp");
     grid_dependency_wait();
@@ -222,9 +222,12 @@ __global__ void __launch_bounds__(kScanThreads, kScanBlocksPerSM) k_scan(const u
             base += __shfl_sync(0xffffffffu, wi, 31);
         }
         __syncthreads();
+        // Entries are clamped to n: a histogram that does not sum to n (never
+        // the case when each step's counts start from zero) cannot send the
+        // candidate walks past the particle arrays.
         const uint32_t ex = ws[warp] + inc - v;
         cell_start[(size_t)t * kScanThreads + threadIdx.x] =
-            make_uint4(ex, ex + q.x, ex + q.x + q.y, ex + q.x + q.y + q.z);
+            make_uint4(min(ex, n), min(ex + q.x, n), min(ex + q.x + q.y, n), min(ex + q.x + q.y + q.z, n));
         q = qn;
     }
 }
@@ -239,7 +242,8 @@ __global__ void k_scatter(const uint2* __restrict__ key_slot, const uint32_t* __
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 ks = key_slot[i];
-    tmp[cell_start[ks.x] + ks.y] = i;
+    const uint32_t at = cell_start[ks.x] + ks.y;
+    if (at < n) tmp[at] = i;  // always, unless the histogram was inconsistent
     counts[ks.x] = 0u;
 }
 
@@ -259,8 +263,10 @@ __global__ void k_rank_gather(const uint2* __restrict__ key_slot, const uint32_t
     uint32_t rank = 0;
     for (uint32_t t = b; t < e; ++t) rank += (tmp[t] < i) ? 1u : 0u;
     const uint32_t dst = b + rank;
-    pos_out[dst] = p;
-    vel_out[dst] = v;
+    if (dst < n) {  // always, unless the histogram was inconsistent
+        pos_out[dst] = p;
+        vel_out[dst] = v;
+    }
 }
 
 // ---------------------------------------------------------------- inspection
@@ -404,7 +410,7 @@ void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimC
 void launch_scan_cells(DeviceState& d, uint32_t /*n*/, cudaStream_t s) {
     const uint32_t blocks = std::min<uint32_t>(d.ntiles, (uint32_t)(kScanBlocksPerSM * sm_count()));
     launch_chained(k_scan, blocks, kScanThreads, s, reinterpret_cast<const uint4*>(d.counts), d.tile_sums, d.ntiles,
-                   reinterpret_cast<uint4*>(d.cell_start));
+                   d.n, reinterpret_cast<uint4*>(d.cell_start));
 }
 
 // Buckets indices by cell and clears the counters.
