@@ -22,6 +22,8 @@ Printed JSON line (rank 0):
              SPH library is not part of the reference) on the host cores.
 
 ``--impl reference`` times that CPU implementation as the reference arm.
+``--only adjoint`` runs the differentiable section alone and prints its record
+(a command to profile; it does not print the bench line).
 """
 from __future__ import annotations
 
