@@ -58,12 +58,10 @@ STAGE_BYTES_PER_PARTICLE = {
 STAGE_BYTES_PER_CELL = {"scan": 4 + 4}  # read the cell histogram, write the cell table
 STEP_BYTES_PER_UPDATE = 213  # canonical whole-step figure (hash 20 + sort 16 + reorder 48 + cells 5 + density 20 + force 44 + integrate 60)
 
-WORKLOADS = {
-    "double_dambreak_1m": dict(scene=17, particleRadius=0.0025, kernelRadius=0.01),
-    "dambreak_16k": dict(scene=16, particleRadius=0.01, kernelRadius=0.04),
-    "dambreak_64k": dict(scene=19, particleRadius=0.005, kernelRadius=0.02),
-    "sphere_pool": dict(scene=18, particleRadius=0.00227, kernelRadius=0.00908),
-}
+# single-scene workloads, batch and adjoint: simplefluid_gb300/workloads/*.json
+from simplefluid_gb300 import configs  # noqa: E402
+
+WORKLOADS = configs.available("scene")
 
 
 def measured_peaks() -> dict:
@@ -137,11 +135,7 @@ class ClockSampler:
 
 
 def make_params(workload: str):
-    from simplefluid_gb300 import SPHParameters
-    w = WORKLOADS[workload]
-    return SPHParameters(particleRadius=w["particleRadius"], kernelRadius=w["kernelRadius"], scene=w["scene"],
-                         pressureStiffness=50.0, viscosity=0.01, restDensity=1000.0, timeStep=1e-4,
-                         boundaryRestitution=0.1)
+    return configs.params(workload)
 
 
 def host_cpu() -> dict:
@@ -192,11 +186,10 @@ def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
     against all contexts interleaved on their own streams.  With several ranks
     the scenes are spread over them (largest first, no communication) and each
     throughput is all ranks' particle-updates over the slowest rank's time."""
-    from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes, shard_batch
-    steps = args.batch_steps
-    base = SPHParameters(particleRadius=0.005, kernelRadius=0.02, pressureStiffness=50.0, viscosity=0.01,
-                         restDensity=1000.0, timeStep=1e-4, boundaryRestitution=0.1)
-    params, counts, pos = batch_cubes(20171, 256, base)
+    from simplefluid_gb300 import SPHBatch, SPHSolver, batch_cubes, shard_batch
+    cfg = configs.load("batched_cubes")
+    steps = args.batch_steps if args.batch_steps else cfg["steps"]
+    params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))
     total_scenes = len(params)
     if ws > 1:
         params, counts, pos, _ = shard_batch(params, counts, pos, rank, ws)
@@ -272,15 +265,15 @@ def measure_adjoint(args) -> dict:
     loss = squared distance of the 32^3 CIC histogram to a seeded target.  Reports
     the plain forward (graph replays, CUDA events), the forward with checkpoints,
     the loss and the adjoint (wall clock, synchronised), and adjoint / forward."""
-    from simplefluid_gb300 import SPHParameters, SPHSolver, scene_positions
-    prm = SPHParameters(particleRadius=0.005, kernelRadius=0.02, scene=19, pressureStiffness=50.0, viscosity=0.01,
-                        restDensity=1000.0, timeStep=1e-4, boundaryRestitution=0.1)
-    pos = scene_positions(prm, 19)
-    rng = np.random.default_rng(20171)
-    vel = rng.normal(scale=0.05, size=pos.shape).astype(np.float32)
-    target = rng.uniform(size=32 ** 3)
+    from simplefluid_gb300 import SPHSolver, scene_positions
+    cfg = configs.load("adjoint_64k")
+    prm = configs.params(cfg)
+    pos = scene_positions(prm, prm.scene, cfg["seed"])
+    rng = np.random.default_rng(cfg["seed"])
+    vel = rng.normal(scale=cfg["initial_velocity_sigma"], size=pos.shape).astype(np.float32)
+    target = rng.uniform(size=cfg["histogram_resolution"] ** 3)
     target = (target / target.sum()).astype(np.float32)
-    steps, ckpt = 200, 20
+    steps, ckpt = cfg["steps"], cfg["checkpoint_every"]
     from simplefluid_gb300 import _capi as C
     lib = C.load()
     with SPHSolver(prm) as s:
@@ -379,7 +372,7 @@ def measure_other_workloads(args, skip: str) -> dict:
     from simplefluid_gb300 import SPHSolver, scene_positions
     from simplefluid_gb300 import _capi as C
     lib = C.load()
-    plan = {"dambreak_16k": 500, "sphere_pool": 100}
+    plan = {wl: configs.load(wl)["steps"] for wl in ("dambreak_16k", "sphere_pool")}
     out = {}
     for wl, steps in plan.items():
         if wl == skip:
@@ -619,7 +612,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-other-workloads", action="store_true")
-    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--batch-steps", type=int, default=0, help="default: the batched_cubes configuration's steps")
     ap.add_argument("--only", choices=["adjoint"], default=None,
                     help="run one section alone and print its record (for profiling); not the bench line")
     args = ap.parse_args()
