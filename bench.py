@@ -186,7 +186,7 @@ def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
     against all contexts interleaved on their own streams.  With several ranks
     the scenes are spread over them (largest first, no communication) and each
     throughput is all ranks' particle-updates over the slowest rank's time."""
-    from simplefluid_gb300 import SPHBatch, SPHSolver, batch_cubes, shard_batch
+    from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes, shard_batch
     cfg = configs.load("batched_cubes")
     steps = args.batch_steps if args.batch_steps else cfg["steps"]
     params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))

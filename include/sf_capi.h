@@ -245,6 +245,17 @@ typedef struct sf_state_report {
 } sf_state_report;
 SF_API sf_status sf_check_state(sf_ctx* ctx, sf_state_report* report);
 
+/* ---- index checks (checked build) -----------------------------------------
+ * The checked build of this library (compiled with SF_DEVICE_CHECKS=1; see
+ * simplefluid_gb300/build.py) checks every cell-table range end and every
+ * neighbour-list entry on the device before it is used; a bad value is
+ * counted and replaced by an in-range one (nothing traps).  *failures
+ * receives the count on the current device since the last reset, and
+ * *compiled_in whether this build has the checks (0: the release build,
+ * *failures = 0).  A non-zero `reset` clears the count.  Either output may be
+ * null. */
+SF_API sf_status sf_index_checks(int32_t reset, uint64_t* failures, int32_t* compiled_in);
+
 /* ---- fault injection (tests) ---------------------------------------------
  * The device allocation `after` allocations from now (0: the next one) fails
  * as out of memory, once; a negative value disarms it.  The call that hits it

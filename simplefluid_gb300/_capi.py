@@ -12,6 +12,11 @@ from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_size_t, c_ui
 
 LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libsimplefluid_gb300.so")
+# the checked build (kernels count bad indices; build(checked=True)); the
+# environment variable SIMPLEFLUID_GB300_CHECKED=1 makes it this process's library
+CHECKED_LIB_PATH = os.path.join(LIB_DIR, "libsimplefluid_gb300_checked.so")
+if os.environ.get("SIMPLEFLUID_GB300_CHECKED") == "1":
+    LIB_PATH = CHECKED_LIB_PATH
 
 SF_OK = 0
 SF_ERR_INVALID_ARGUMENT = 1
@@ -143,6 +148,7 @@ PROTOTYPES = {
     "sf_get_state_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
     "sf_device_state": (c_int32, [c_void_p, _P(sf_device_view)]),
     "sf_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
+    "sf_index_checks": (c_int32, [c_int32, _P(ctypes.c_uint64), _P(c_int32)]),
     "sf_test_fail_allocation": (c_int32, [ctypes.c_int64]),
     "sf_batch_check_state": (c_int32, [c_void_p, _P(sf_state_report)]),
     "sf_get_num_particles": (c_int32, [c_void_p, _P(c_uint32)]),
@@ -213,6 +219,15 @@ def load(path: str | None = None) -> ctypes.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+def index_checks(reset: bool = False) -> tuple:
+    """(bad indices counted on the current device, whether this library is the
+    checked build); `reset` clears the count (sf_index_checks)."""
+    lib = load()
+    failures, compiled = ctypes.c_uint64(), c_int32()
+    check(lib.sf_index_checks(1 if reset else 0, ctypes.byref(failures), ctypes.byref(compiled)))
+    return int(failures.value), bool(compiled.value)
 
 
 def check(status: int) -> None:

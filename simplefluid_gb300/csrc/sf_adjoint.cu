@@ -31,22 +31,22 @@ constexpr int kAdjBlock = 128;
 // candidate cells when the list overflowed.
 template <int kReach, typename F>
 __device__ __forceinline__ void for_neighbours(const SimConst& c, uint32_t i, const float4& xi,
-                                               const float4* __restrict__ pos, const uint32_t* __restrict__ cs,
-                                               const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ cnt,
-                                               F&& f) {
+                                               const float4* __restrict__ pos, uint32_t n,
+                                               const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr,
+                                               const uint32_t* __restrict__ cnt, F&& f) {
     const uint32_t m = __ldg(cnt + i);
     if (m <= (uint32_t)kNbCap) {
         const uint32_t* lst = nbr + nbr_index(i, 0);  // slot k at lst[k * kNbTile]
         uint32_t jn = __ldg(lst);
         for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t j = jn;
+            const uint32_t j = checked_index(jn, n);
             // the next index is in flight while this neighbour is processed
             // (slots past the count hold stale values, never used)
             jn = __ldg(lst + (size_t)min(k + 1, (uint32_t)kNbCap - 1) * kNbTile);
             if (j != i) f(j, ldg4(pos + j));  // the list records the particle itself
         }
     } else {
-        for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+        for_candidates<kReach>(c, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             if (j == i) return;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2) f(j, xj);
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kAdjBlock)
         // while a neighbour is processed.  The list holds the particle itself
         // (skipped); slots past the count hold stale values, never used.
         const uint32_t* lst = nbr + nbr_index(k, 0);  // slot s at lst[s * kNbTile]
-        uint32_t jc = __ldg(lst), jn = __ldg(lst + kNbTile);
+        uint32_t jc = checked_index(__ldg(lst), n), jn = __ldg(lst + kNbTile);
         float4 nx, nv, na, nb;
         if (m) {
             ld8(pv + 2 * (size_t)jc, nx, nv);
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kAdjBlock)
             const uint32_t j = jc;
             const float4 xj = nx, vj = nv, apbj = na, avbj = nb;
             if (s + 1 < m) {
-                jc = jn;
+                jc = checked_index(jn, n);
                 jn = __ldg(lst + (size_t)min(s + 2, (uint32_t)kNbCap - 1) * kNbTile);
                 ld8(pv + 2 * (size_t)jc, nx, nv);
                 ld8(ab + 2 * (size_t)jc, na, nb);
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kAdjBlock)
             if (j != k) pair(xj, vj, apbj, avbj);
         }
     } else {
-        for_candidates<kReach>(c, cs, pos, xk.x, xk.y, xk.z, [&](uint32_t j, const float4& xp) {
+        for_candidates<kReach>(c, cs, pos, n, xk.x, xk.y, xk.z, [&](uint32_t j, const float4& xp) {
             if (j == k) return;
             const float dx = xk.x - xp.x, dy = xk.y - xp.y, dz = xk.z - xp.z;
             if (!(fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)) return;
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kAdjBlock)
     const float4 xk = pos[k];
     const float rbk = xrb[k].w;
     float x0 = 0.f, x1 = 0.f, x2 = 0.f;
-    for_neighbours<kReach>(c, k, xk, pos, cs, nbr, cnt, [&](uint32_t j, const float4&) {
+    for_neighbours<kReach>(c, k, xk, pos, n, cs, nbr, cnt, [&](uint32_t j, const float4&) {
         const float4 xj = ldg4(xrb + j);  // position and rho_bar in one load
         const float d0 = xk.x - xj.x, d1 = xk.y - xj.y, d2 = xk.z - xj.z;
         const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
@@ -425,6 +425,8 @@ __global__ void k_hist_grad(const float4* __restrict__ pos, uint32_t n, SimConst
 }
 
 }  // namespace
+
+SF_INDEX_CHECK_ACCESSOR(index_check_failures_adjoint)
 
 // ------------------------------------------------------------------ launchers
 void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,

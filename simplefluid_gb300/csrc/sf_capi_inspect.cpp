@@ -94,6 +94,19 @@ SF_API sf_status sf_neighbour_stats(sf_ctx* ctx, uint32_t* count, uint32_t* hash
     return SF_OK;
 }
 
+SF_API sf_status sf_index_checks(int32_t reset, uint64_t* failures, int32_t* compiled_in) {
+#ifndef SF_DEVICE_CHECKS
+#define SF_DEVICE_CHECKS 0
+#endif
+    if (compiled_in) *compiled_in = SF_DEVICE_CHECKS;
+    const bool r = reset != 0;
+    const uint64_t total = sf::index_check_failures_density(r) + sf::index_check_failures_force(r) +
+                           sf::index_check_failures_adjoint(r) + sf::index_check_failures_grid(r);
+    if (failures) *failures = total;
+    if (SF_DEVICE_CHECKS) SF_TRY(check_launch("sf_index_checks"));
+    return SF_OK;
+}
+
 SF_API sf_status sf_test_fail_allocation(int64_t after) {
     set_fail_allocation(after);
     return SF_OK;

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kBlockSize)
         const float4 xi = pos[i];
         float s = 0.f;
         uint32_t* const lst = kMode == kEmitTile ? nbr + nbr_index(i, 0) : nullptr;  // slot k at lst[k * kNbTile]
-        for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+        for_candidates<kReach>(c, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             const bool near = r2 < c.h2;
@@ -93,6 +93,8 @@ void density_as(const DeviceState& d, const SimConst& c, cudaStream_t s) {
 }
 
 }  // namespace
+
+SF_INDEX_CHECK_ACCESSOR(index_check_failures_density)
 
 void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s) {
     if (!d.n) return;

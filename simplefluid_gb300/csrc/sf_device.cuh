@@ -109,6 +109,58 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {  // murmur3 finaliser
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+// Index checks of the checked build (compiled with SF_DEVICE_CHECKS=1; the
+// release build compiles them out).  Every cell-table range end and every
+// neighbour-list entry is checked against the particle count before it is
+// used: a bad value is counted in this translation unit's counter and
+// replaced by an in-range one, so the access stays inside its array and
+// nothing traps.  sf_index_checks() reads and resets the counters.
+#ifndef SF_DEVICE_CHECKS
+#define SF_DEVICE_CHECKS 0
+#endif
+#if SF_DEVICE_CHECKS
+static __device__ unsigned long long g_index_check_failures;  // one per translation unit
+#endif
+// j, a particle index, where j < n; else 0 (counted)
+__device__ __forceinline__ uint32_t checked_index(uint32_t j, uint32_t n) {
+#if SF_DEVICE_CHECKS
+    if (j >= n) {
+        atomicAdd(&g_index_check_failures, 1ull);
+        return 0u;
+    }
+#endif
+    (void)n;
+    return j;
+}
+// v, a cell-table entry (a range end), where v <= n; else n (counted)
+__device__ __forceinline__ uint32_t checked_end(uint32_t v, uint32_t n) {
+#if SF_DEVICE_CHECKS
+    if (v > n) {
+        atomicAdd(&g_index_check_failures, 1ull);
+        return n;
+    }
+#endif
+    (void)n;
+    return v;
+}
+// Host accessor of this translation unit's counter: fn(reset) returns it
+// (0 in the release build) and clears it when `reset`.
+#if SF_DEVICE_CHECKS
+#define SF_INDEX_CHECK_ACCESSOR(fn)                                                               \
+    uint64_t fn(bool reset) {                                                                    \
+        unsigned long long v = 0;                                                                \
+        cudaMemcpyFromSymbol(&v, g_index_check_failures, sizeof(v));                             \
+        if (reset) {                                                                             \
+            const unsigned long long z = 0;                                                      \
+            cudaMemcpyToSymbol(g_index_check_failures, &z, sizeof(z));                           \
+        }                                                                                        \
+        return v;                                                                                \
+    }
+#else
+#define SF_INDEX_CHECK_ACCESSOR(fn) \
+    uint64_t fn(bool) { return 0; }
+#endif
+
 // Counting-sort histogram: the particle's arrival slot in its cell, and the
 // cell's scan tile total (one atomic per distinct tile per warp).  Call with
 // every live lane of the warp converged.
@@ -144,8 +196,8 @@ __device__ __forceinline__ float face_gap(float off, int d, float w, float margi
 // for_candidate_rows calls g(b, e) with the sorted index range [b, e) of each
 // candidate row in that order (ranges of rows out of reach are empty).
 template <int kReach, typename G>
-__device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint32_t* __restrict__ cs, float x,
-                                                   float y, float z, G&& g) {
+__device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint32_t* __restrict__ cs, uint32_t n,
+                                                   float x, float y, float z, G&& g) {
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
     const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
     const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
@@ -189,8 +241,8 @@ __device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint
             const int x1 = (kReach > 1 && g2 + ghi2 >= c.prune_h2) ? xb1 : xb;
             const uint32_t* row = plane + dy * (int)n0;
             const bool live = g2 < c.prune_h2;
-            rb[dy + kReach] = live ? __ldg(row + x0) : 0u;
-            re[dy + kReach] = live ? __ldg(row + x1 + 1) : 0u;
+            rb[dy + kReach] = live ? checked_end(__ldg(row + x0), n) : 0u;
+            re[dy + kReach] = live ? checked_end(__ldg(row + x1 + 1), n) : 0u;
         }
 #pragma unroll
         for (int dy = 0; dy <= 2 * kReach; ++dy) g(rb[dy], re[dy]);
@@ -199,8 +251,9 @@ __device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint
 
 template <int kReach, typename F>
 __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
-                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
-    for_candidate_rows<kReach>(c, cs, x, y, z, [&](uint32_t b, uint32_t e) {
+                                               const float4* __restrict__ pos, uint32_t n, float x, float y, float z,
+                                               F&& f) {
+    for_candidate_rows<kReach>(c, cs, n, x, y, z, [&](uint32_t b, uint32_t e) {
         uint32_t j = b;
 #pragma unroll 1
         for (; j + 1 < e; j += 2) {
@@ -223,7 +276,8 @@ __device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool pred) {
 // per row.
 template <int kReach, typename F>
 __device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const uint32_t* __restrict__ cs,
-                                               const float4* __restrict__ pos, float x, float y, float z, F&& f) {
+                                               const float4* __restrict__ pos, uint32_t n, float x, float y, float z,
+                                               F&& f) {
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
     const int cy = cell_coord(y, c.bmin[1], c.inv_cell[1], c.n[1]);
     const int cz = cell_coord(z, c.bmin[2], c.inv_cell[2], c.n[2]);
@@ -251,7 +305,7 @@ __device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const u
             }
             const int x0 = max(cx + lo, 0), x1 = min(cx + hi, c.n[0] - 1);
             const uint32_t row = c.cell_base + ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
-            const uint32_t b = __ldg(cs + row + x0), e = __ldg(cs + row + x1 + 1);
+            const uint32_t b = checked_end(__ldg(cs + row + x0), n), e = checked_end(__ldg(cs + row + x1 + 1), n);
 #pragma unroll 1
             for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
         }

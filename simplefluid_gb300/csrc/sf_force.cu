@@ -24,7 +24,8 @@ template <bool kUseList, int kPrefetch, bool kIntegrate, int kReach, bool kBatch
 __device__ __forceinline__ void force_one(
     uint32_t i, const float4* __restrict__ pos, const float4* __restrict__ vel, const float2* __restrict__ pr,
     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-    const float4* __restrict__ pv, const SimConst& c0, const SimConst* __restrict__ table, const uint32_t* __restrict__ scene_off, uint32_t nscenes,
+    const float4* __restrict__ pv, uint32_t n, const SimConst& c0, const SimConst* __restrict__ table,
+    const uint32_t* __restrict__ scene_off, uint32_t nscenes,
     float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint32_t* __restrict__ counts,
     uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
     float4* __restrict__ sums, const FrameState* __restrict__ frame, uint32_t& v2, uint32_t& a2) {
@@ -51,7 +52,7 @@ __device__ __forceinline__ void force_one(
                 jn[u] = __ldg(lst + (size_t)min(k + kPrefetch + u, (uint32_t)kNbCap - 1) * kNbTile);
             }
 #pragma unroll
-            for (int u = 0; u < kPrefetch; ++u) ld8(pv + 2 * (size_t)j[u], xj[u], vj[u]);
+            for (int u = 0; u < kPrefetch; ++u) ld8(pv + 2 * (size_t)checked_index(j[u], n), xj[u], vj[u]);
 #pragma unroll
             for (int u = 0; u < kPrefetch; ++u)
                 pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
@@ -60,12 +61,12 @@ __device__ __forceinline__ void force_one(
         float4 xj[kPrefetch - 1], vj[kPrefetch - 1];
 #pragma unroll
         for (int u = 0; u < kPrefetch - 1; ++u)
-            if (k + u < cnt) ld8(pv + 2 * (size_t)jn[u], xj[u], vj[u]);
+            if (k + u < cnt) ld8(pv + 2 * (size_t)checked_index(jn[u], n), xj[u], vj[u]);
 #pragma unroll
         for (int u = 0; u < kPrefetch - 1; ++u)
             if (k + u < cnt) pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
     } else {
-        for_candidates_rolled<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+        for_candidates_rolled<kReach>(c, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             if (j == i) return;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
             if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(kBlockSize)
     const uint32_t i = blockIdx.x * kBlockSize + threadIdx.x;
     uint32_t v2 = 0u, a2 = 0u;
     if (i < n)
-        force_one<kUseList, kPrefetch, kIntegrate, kReach, kBatched>(i, pos, vel, pr, cs, nbr, nbr_count, pv, c0, table,
+        force_one<kUseList, kPrefetch, kIntegrate, kReach, kBatched>(i, pos, vel, pr, cs, nbr, nbr_count, pv, n, c0, table,
                                                                      scene_off, nscenes, pos_out, vel_out, counts,
                                                                      tile_sums, key_slot, acc_out, sums, frame, v2, a2);
     if (!kBatched && kIntegrate && frame && c0.adaptive) {
@@ -184,6 +185,8 @@ void launch_force(DeviceState& d, const SimConst& c, cudaStream_t s) {
 }
 
 }  // namespace
+
+SF_INDEX_CHECK_ACCESSOR(index_check_failures_force)
 
 void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s) { launch_force<true>(d, c, s); }
 

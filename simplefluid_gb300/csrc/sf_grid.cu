@@ -279,7 +279,7 @@ __global__ void k_neighbour_stats(const float4* __restrict__ pos, const uint32_t
     const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
     const float4 xi = pos[i];
     uint32_t cnt = 0, h = 0;
-    for_candidates<kReach>(c, cs, pos, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+    for_candidates<kReach>(c, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
         if (j == i) return;
         const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
         if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2) {
@@ -339,6 +339,8 @@ __global__ void k_check_ids(const uint32_t* __restrict__ seen, uint32_t n, uint3
 }
 
 }  // namespace
+
+SF_INDEX_CHECK_ACCESSOR(index_check_failures_grid)
 
 // ---------------------------------------------------------------- launchers
 void launch_check_state(const DeviceState& d, const SimConst& c, const uint32_t* nbr_count, uint32_t* seen,

@@ -140,6 +140,13 @@ void launch_density(const DeviceState& d, const SimConst& c, cudaStream_t s);
 void launch_force_integrate(DeviceState& d, const SimConst& c, cudaStream_t s);
 // forces only: acceleration into d.accel (inspection)
 void launch_force_only(DeviceState& d, const SimConst& c, cudaStream_t s);
+
+// Index-check failures counted by the checked build's kernels, per
+// translation unit (always 0 in the release build); `reset` clears them.
+uint64_t index_check_failures_density(bool reset);
+uint64_t index_check_failures_force(bool reset);
+uint64_t index_check_failures_adjoint(bool reset);
+uint64_t index_check_failures_grid(bool reset);
 void launch_keys(const DeviceState& d, const float4* pos, uint32_t n, const SimConst& c, uint32_t* keys,
                  cudaStream_t s);
 // State invariants for sf_check_state: `seen` is n words of scratch, `report`
