@@ -50,3 +50,24 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["unit"] == "particle-updates/s" and d["value"] > 0
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_batched_and_adjoint_sections():
+    """The batched section (sharding, autotuning, sequential and interleaved
+    comparisons, CPU sample) and the adjoint section run from their workload
+    configurations and report their records."""
+    d = _run("--steps", "5", "--warmup", "3", "--cpu-seconds", "1", "--batch-steps", "3", "--no-other-workloads")
+    b = d["batched"]
+    assert b["scenes"] == 256 and b["steps"] == 3 and b["value"] > 0 and b["ratio_vs_sequential"] > 1
+    assert b["cpu_baseline"]["value"] > 0 and b["cpu_baseline"]["kind"] == "port"
+    a = d["adjoint"]
+    assert a["particles"] == 65536 and a["steps"] == 200 and a["ckpt_every"] == 20
+    assert 0 < a["ratio_adjoint_over_forward"] < 10 and a["loss"] > 0
+
+
+def test_only_adjoint_prints_its_record():
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--only", "adjoint"], capture_output=True,
+                         text=True, cwd=ROOT, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    rec = json.loads([ln for ln in out.stdout.splitlines() if ln.startswith("{")][-1])
+    assert rec["section"] == "adjoint" and rec["adjoint_ms"] > 0
