@@ -140,6 +140,7 @@ SF_API sf_status sf_batch_get_params(const sf_batch* b, uint32_t scene, sf_param
 }
 
 SF_API sf_status sf_batch_set_state(sf_batch* b, const uint32_t* counts, const float* pos_xyz, const float* vel_xyz) {
+    SF_RANGE("sf_batch_set_state");
     SF_TRY(need_batch(b));
     if (!counts) return fail(SF_ERR_INVALID_ARGUMENT, "null counts");
     const size_t ns = b->params.size();
@@ -157,6 +158,7 @@ SF_API sf_status sf_batch_set_state(sf_batch* b, const uint32_t* counts, const f
 }
 
 SF_API sf_status sf_batch_get_state(sf_batch* b, float* pos_xyz, float* vel_xyz, uint32_t n) {
+    SF_RANGE("sf_batch_get_state");
     SF_TRY(need_batch(b));
     return sf_get_state(&b->eng, pos_xyz, vel_xyz, n);
 }
@@ -167,6 +169,7 @@ SF_API sf_status sf_batch_num_particles(const sf_batch* b, uint32_t* n_out) {
 }
 
 SF_API sf_status sf_batch_step(sf_batch* b, uint32_t nsteps) {
+    SF_RANGE("sf_batch_step");
     SF_TRY(need_batch(b));
     return sf_step(&b->eng, nsteps);
 }
@@ -183,6 +186,7 @@ SF_API sf_status sf_batch_synchronize(sf_batch* b) {
 
 SF_API sf_status sf_batch_step_timed(sf_batch* b, uint32_t nsteps, uint64_t flush_bytes, float* total_ms,
                                      float* step_ms) {
+    SF_RANGE("sf_batch_step");
     SF_TRY(need_batch(b));
     return sf_step_timed(&b->eng, nsteps, flush_bytes, total_ms, step_ms);
 }
