@@ -366,12 +366,21 @@ struct PairAcc {
     float apx = 0.f, apy = 0.f, apz = 0.f, avx = 0.f, avy = 0.f, avz = 0.f;
 };
 
-__device__ __forceinline__ void pair_terms(const SimConst& c, const float4& xi, const float4& vi, float pi,
+// A pointer the compiler cannot see through, so loads through it are issued
+// where they are written (not hoisted, not merged with earlier loads).
+template <typename T>
+__device__ __forceinline__ const T* opaque_ptr(const T* p) {
+    const T* r;
+    asm volatile("mov.b64 %0, %1;" : "=l"(r) : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ void pair_terms(float h, const float4& xi, const float4& vi, float pi,
                                            const float4& xj, const float2& prj, const float4& vj, PairAcc& a) {
     const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float r = sqrtf(r2);
-    const float hr = c.h - r;
+    const float hr = h - r;
     const float w = hr * prj.y;
     a.avx = fmaf(w, vj.x - vi.x, a.avx);
     a.avy = fmaf(w, vj.y - vi.y, a.avy);

@@ -30,7 +30,15 @@ __device__ __forceinline__ void force_one(
     uint32_t* __restrict__ tile_sums, uint2* __restrict__ key_slot, float4* __restrict__ acc_out,
     float4* __restrict__ sums, const FrameState* __restrict__ frame, uint32_t& v2, uint32_t& a2) {
     static_assert(kPrefetch >= 2, "the list tail holds up to kPrefetch - 1 neighbours");
-    const SimConst c = const_of<kBatched>(c0, table, scene_off, nscenes, i);
+    // A batch reads its scene's constants where they are used (the kernel
+    // radius before the neighbour loop, the rest after it) instead of
+    // holding them in registers across the loop.
+    const uint32_t scene = kBatched ? scene_of(scene_off, nscenes, i) : 0u;
+    auto consts = [&]() -> SimConst {
+        if constexpr (kBatched) return *opaque_ptr(table + scene);
+        else return c0;
+    };
+    const float h = kBatched ? opaque_ptr(table + scene)->h : c0.h;
     const float4 xi = pos[i];
     const float4 vi = vel[i];
     const float2 pri = pr[i];
@@ -55,7 +63,7 @@ __device__ __forceinline__ void force_one(
             for (int u = 0; u < kPrefetch; ++u) ld8(pv + 2 * (size_t)checked_index(j[u], n), xj[u], vj[u]);
 #pragma unroll
             for (int u = 0; u < kPrefetch; ++u)
-                pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
+                pair_terms(h, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
         }
         // the last cnt - k < kPrefetch neighbours: their indices are in jn
         float4 xj[kPrefetch - 1], vj[kPrefetch - 1];
@@ -64,15 +72,17 @@ __device__ __forceinline__ void force_one(
             if (k + u < cnt) ld8(pv + 2 * (size_t)checked_index(jn[u], n), xj[u], vj[u]);
 #pragma unroll
         for (int u = 0; u < kPrefetch - 1; ++u)
-            if (k + u < cnt) pair_terms(c, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
+            if (k + u < cnt) pair_terms(h, xi, vi, pri.x, xj[u], make_float2(xj[u].w, vj[u].w), vj[u], a);
     } else {
-        for_candidates_rolled<kReach>(c, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
+        const SimConst cr = consts();
+        for_candidates_rolled<kReach>(cr, cs, pos, n, xi.x, xi.y, xi.z, [&](uint32_t j, const float4& xj) {
             if (j == i) return;
             const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-            if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < c.h2)
-                pair_terms(c, xi, vi, pri.x, xj, __ldg(pr + j), ldg4(vel + j), a);
+            if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < cr.h2)
+                pair_terms(cr.h, xi, vi, pri.x, xj, __ldg(pr + j), ldg4(vel + j), a);
         });
     }
+    const SimConst c = consts();
     if (sums) {
         sums[2 * (size_t)i] = make_float4(a.apx, a.apy, a.apz, 0.f);
         sums[2 * (size_t)i + 1] = make_float4(a.avx, a.avy, a.avz, 0.f);
