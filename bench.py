@@ -417,24 +417,44 @@ def dist_env():
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def workload_config(workload: str, prm, n: int, grid, ws: int) -> dict:
+    """The `config` object of both arms' lines (the same keys and values)."""
+    return {"workload": workload, "particles": int(n), "kernel_radius": prm.kernelRadius,
+            "particle_radius": prm.particleRadius, "dt": prm.timeStep, "grid": [int(g) for g in grid],
+            "parallelism": f"replicas{ws}" if ws > 1 else "single",
+            "l2": "flushed before every timed GPU step (256 MiB write outside the timed intervals); "
+                  "the state (0.4 GB at 1M particles) exceeds the 129 MB L2"}
+
+
 def run_reference(args, workload):
+    """The reference arm: the CPU restatement of the SPH step (the reference's
+    own solver library is not part of the reference tree), on all host
+    threads, over the same workload, warm-up and step count as the GPU arm.
+    Its input comes from the oracle's scene generator, which reproduces the
+    reference's Source/SceneManager.cpp bit for bit; nothing of the product
+    library is loaded."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from simplefluid_gb300 import scene_positions
+    from oracle import oracle as O
+    O.build()
+    cfg = configs.load(workload)
     prm = make_params(workload)
-    pos = scene_positions(prm, prm.scene)
-    budget = min(120.0, max(10.0, 1.0 * args.steps))
-    rate, steps, threads = cpu_oracle_rate(pos, prm, budget, args.steps, warmup=min(args.warmup, 2))
+    cp = prm.to_c()
+    pos = O.scene(cp, prm.scene, cfg["seed"])
+    d = O.derive(cp)
+    grid = (d["nx"], d["ny"], d["nz"])
+    budget = min(240.0, max(10.0, 1.0 * args.steps))
+    rate, steps, threads = cpu_oracle_rate(pos, prm, budget, args.steps, warmup=args.warmup)
     sample = (f"{steps} of {args.steps} sub-steps of the {pos.shape[0]}-particle {workload} "
-              f"(after {min(args.warmup, 2)} warm-up), time-bounded at {budget:.0f} s")
+              f"(after {args.warmup} warm-up), time-bounded at {budget:.0f} s")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-        "warmup": min(args.warmup, 2), "ms_per_step": 1e3 * pos.shape[0] / rate, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * pos.shape[0] / rate, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded scene generator)",
-        "config": {"workload": workload, "particles": int(pos.shape[0]), "kernel_radius": prm.kernelRadius,
-                   "particle_radius": prm.particleRadius, "dt": prm.timeStep},
+        "data": "synthetic (seeded scene generator: jittered lattice blocks, seed 20171)",
+        "config": workload_config(workload, prm, pos.shape[0], grid, ws),
+        "gpu_launches": 0,
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                          "note": "CPU restatement (reference TBB solver library unavailable: not in the reference tree)",
                          "host": host_cpu()},
@@ -450,7 +470,7 @@ def run_ours(args, workload):
     lib = C.load()
     C.check(lib.sf_select_device(local_rank))
     prm = make_params(workload)
-    pos = scene_positions(prm, prm.scene)
+    pos = scene_positions(prm, prm.scene, configs.load(workload)["seed"])
     n = pos.shape[0]
     solver = SPHSolver(prm)
     solver.setParticles(pos)
@@ -569,10 +589,7 @@ def run_ours(args, workload):
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded scene generator: jittered lattice blocks, seed 20171)",
-        "config": {"workload": workload, "particles": int(n), "kernel_radius": prm.kernelRadius,
-                   "particle_radius": prm.particleRadius, "dt": prm.timeStep, "grid": [nx, ny, nz],
-                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                   "l2": "flushed before every timed step (256 MiB write outside the timed intervals)"},
+        "config": workload_config(workload, prm, n, (nx, ny, nz), ws),
         "value_warm_l2": ws * n * args.steps / (max_over_ranks(warm_ms.value) * 1e-3),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,

@@ -1,11 +1,13 @@
 #!/bin/sh
 # Compile the reference's own scene generator (Source/SceneManager.cpp, read in
-# place from the read-only reference tree) with the shim headers in ref_shim/
+# place from a read-only reference tree) with the shim headers in ref_shim/
 # into oracle/_ref/libref_scenes.so.  The solver itself (Banana SPHSolver) is
 # not part of the reference tree and cannot be built.  Test infrastructure only.
+# Usage: build_ref.sh <reference root>   (or SF_REFERENCE_ROOT in the environment)
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${SF_REFERENCE_ROOT:-/root/reference}"
+REF="${1:-$SF_REFERENCE_ROOT}"
+[ -n "$REF" ] || { echo "usage: build_ref.sh <reference root> (or set SF_REFERENCE_ROOT)" >&2; exit 2; }
 [ -f "$REF/Source/SceneManager.cpp" ] || { echo "reference tree not present: $REF" >&2; exit 1; }
 mkdir -p "$HERE/_ref"
 ${CXX:-g++} -std=c++17 -O2 -fPIC -shared -ffp-contract=off -fno-fast-math \

@@ -32,10 +32,16 @@ def build(force: bool = False) -> str:
     return ORACLE_LIB
 
 
-def build_ref() -> str | None:
-    """Compile the reference scene generator when the reference tree is here."""
+def build_ref(ref_root: str | None = None) -> str | None:
+    """Compile the reference's scene generator from the reference tree at
+    `ref_root` (else $SF_REFERENCE_ROOT) into oracle/_ref.  Without a tree,
+    an earlier build is used when present.  Returns the library path, or
+    None when there is neither."""
+    root = ref_root or os.environ.get("SF_REFERENCE_ROOT")
+    if not root:
+        return REF_LIB if os.path.exists(REF_LIB) else None
     try:
-        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")],
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), root],
                               stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     except (subprocess.CalledProcessError, OSError):
         return None

@@ -12,8 +12,9 @@
    which is absent) and let a run on another host architecture check that its
    oracle build computes the same bits.
 
-Run from the repository root when the reference tree is present:
-    python tests/golden/make_golden.py
+Run from the repository root with the reference tree's location:
+    python tests/golden/make_golden.py <reference root>
+(or with SF_REFERENCE_ROOT set).
 """
 from __future__ import annotations
 
@@ -60,7 +61,7 @@ def small_params() -> sf_params:
 
 def main() -> None:
     O.build(force=True)
-    if O.build_ref() is None:
+    if O.build_ref(sys.argv[1] if len(sys.argv) > 1 else None) is None:
         raise SystemExit("reference tree not available: cannot build oracle/_ref")
     out = {}
     for s, r in REF_CASES:

@@ -110,3 +110,31 @@ def test_batch_rejects_mixed_grids():
         SPHBatch([a, b])
     with pytest.raises(C.SFError):
         SPHBatch([small_base(cellsPerH=3).to_c()])
+
+
+@pytest.mark.gpu
+def test_batched_cubes_workload_500_steps(oracle):
+    """The batched-cube workload as configured (256 scenes, counts log-uniform
+    in [2000, 65536], 500 sub-steps): after the 500 sub-steps every sampled
+    scene (every 16th, the smallest and the largest) equals the oracle run on
+    that scene alone, bit for bit, and the whole batch passes the state checks."""
+    from simplefluid_gb300 import configs
+    cfg = configs.load("batched_cubes")
+    assert cfg["scenes"] == 256 and cfg["steps"] == 500
+    params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))
+    with SPHBatch(params) as b:
+        b.setState(counts, pos)
+        b.step(cfg["steps"])
+        gpos, gvel = b.getState()
+        rep = b.checkState()
+    assert all(rep[k] == 0 for k in ("non_finite", "outside_box", "unsorted", "cell_table_mismatch", "bad_ids"))
+    slices = _scene_slices(counts)
+    sample = sorted(set(range(0, len(params), 16)) | {int(np.argmin(counts)), int(np.argmax(counts))})
+    for s in sample:
+        sl = slices[s]
+        st = oracle.State(pos[sl])
+        st.step(params[s], cfg["steps"])
+        st.sort(params[s])
+        opos, ovel = st.original_order()
+        assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
+        assert np.array_equal(gvel[sl].view(np.uint32), ovel.view(np.uint32)), s

@@ -44,9 +44,11 @@ def test_oracle_scenes_match_reference_golden(oracle):
 
 
 def test_oracle_scenes_match_compiled_reference_live(oracle):
-    """When the reference tree is present, compare against it directly too."""
+    """Where the reference's own scene generator was built (oracle/_ref, by
+    the build entry point on a machine holding the reference tree), compare
+    against it directly too."""
     if oracle.build_ref() is None:
-        pytest.skip("reference tree not available here")
+        pytest.skip("the reference's scene generator is not built on this machine")
     for s in range(4):
         for r in (0.03, 0.011, 0.0075):
             a = oracle.scene(_cparams(r), s)

@@ -352,6 +352,61 @@ def test_full_size_1m_double_dambreak(oracle):
     assert np.all(gpos >= np.float32(0.0025)) and np.all(gpos <= np.float32(0.9975))
 
 
+def _assert_same_state_bits(s, st, what):
+    """The solver's state equals the oracle's bit for bit, in the same sorted
+    order (the solver re-sorts after every sub-step; the oracle is re-sorted
+    here the same way)."""
+    gpos, gvel = s.getState()
+    _, _, gids, _ = s.sortedState()
+    opos, ovel = st.original_order()
+    assert np.array_equal(gids, st.ids), what
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32)), what
+    assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32)), what
+    return gpos, gvel
+
+
+def test_1m_double_dambreak_1000_steps_bit_identical(oracle):
+    """The 1,048,576-particle double dambreak over its 1,000 sub-steps: after
+    every 100 sub-steps the sorted order, positions and velocities equal the
+    oracle's bit for bit, and kinetic energy and mean density error are
+    inside the stated band of the oracle's (the band is implied by the bit
+    equality; it is computed so that a tolerance failure names its size)."""
+    prm = params_1m()
+    pos = scene_positions(prm, C.SF_SCENE_DOUBLE_DAMBREAK_1M)
+    assert pos.shape[0] == 1048576
+    st = oracle.State(pos)
+    cp = prm.to_c()
+    with solver_with(prm, pos) as s:
+        for chunk in range(10):
+            s.step(100)
+            st.step(cp, 100)
+            st.sort(cp)
+            gpos, gvel = _assert_same_state_bits(s, st, f"after {100 * (chunk + 1)} sub-steps")
+            opos, ovel = st.original_order()
+            gke, gde = _ke_and_density_error(gpos, gvel, prm, oracle)
+            oke, ode = _ke_and_density_error(opos, ovel, prm, oracle)
+            assert abs(gke - oke) <= TRAJ_BAND * max(oke, 1e-12), (chunk, gke, oke)
+            assert abs(gde - ode) <= TRAJ_BAND * max(ode, 1e-12) + 1e-7, (chunk, gde, ode)
+        assert oke > 0 and ode > 0  # the fluid moves and compresses
+        rep = s.checkState()
+        assert all(rep[k] == 0 for k in ("non_finite", "outside_box", "unsorted", "cell_table_mismatch", "bad_ids"))
+
+
+def test_sphere_pool_50_steps_bit_identical(oracle):
+    """Sphere drop into a pool (~3.35M particles) over 50 sub-steps: the state
+    equals the oracle's bit for bit after 10 and after 50 sub-steps."""
+    prm = params_1m(particleRadius=0.00227, kernelRadius=0.00908, scene=C.SF_SCENE_SPHERE_POOL)
+    pos = scene_positions(prm, C.SF_SCENE_SPHERE_POOL)
+    st = oracle.State(pos)
+    cp = prm.to_c()
+    with solver_with(prm, pos) as s:
+        for chunk in (10, 40):
+            s.step(chunk)
+            st.step(cp, chunk)
+            st.sort(cp)
+            _assert_same_state_bits(s, st, f"after {chunk} more sub-steps")
+
+
 def _tuned_run(prm, pos, tune, steps):
     import ctypes
     lib = C.load()
@@ -423,13 +478,38 @@ def test_full_size_sphere_pool(oracle):
     assert np.all(gpos >= lo) and np.all(gpos <= hi)
 
 
+def _sampled_all_pairs_densities(spos, sample, h):
+    """FP64 sum of (h^2 - r^2)^3 over all particles within h of each sampled
+    particle, found by bucketing every particle into cells of edge h (numpy
+    only): the neighbours of a particle lie in its own and the 26 adjacent
+    cells."""
+    p = spos.astype(np.float64)
+    cell = np.floor(p / h).astype(np.int64) + 1  # >= 1, so the -1 neighbours stay >= 0
+    dims = cell.max(0) + 2
+    key = (cell[:, 2] * dims[1] + cell[:, 1]) * dims[0] + cell[:, 0]
+    order = np.argsort(key, kind="stable")
+    skey = key[order]
+    out = []
+    for i in sample:
+        cx, cy, cz = cell[i]
+        parts = []
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                k0 = ((cz + dz) * dims[1] + (cy + dy)) * dims[0] + (cx - 1)
+                lo, hi = np.searchsorted(skey, [k0, k0 + 3])
+                parts.append(order[lo:hi])
+        nb = np.concatenate(parts)
+        r2 = ((p[nb] - p[i]) ** 2).sum(1)
+        out.append(((h * h - r2[r2 < h * h]) ** 3).sum())
+    return np.array(out)
+
+
 def test_large_scale_16m_lattice(oracle):
     """16,000,000 particles (a 200 x 400 x 200 jittered lattice, 72M grid
     cells): after 5 steps the state checks are clean (sorted, permutation,
     cell table, inside the box, finite), and the densities of 200 sampled
-    particles equal all-pairs sums over their kd-tree neighbourhoods (FP64,
+    particles equal all-pairs sums over their cell neighbourhoods (FP64,
     within the FP32 summation-order band)."""
-    spatial = pytest.importorskip("scipy.spatial")
     r = 0.0012
     prm = params_16k(particleRadius=r, kernelRadius=4 * r)
     rng = np.random.default_rng(16)
@@ -448,13 +528,9 @@ def test_large_scale_16m_lattice(oracle):
         spos, _, ids, _ = s.sortedState()
     h = np.float64(np.float32(4 * r))
     d = oracle.derive(prm.to_c())
-    tree = spatial.cKDTree(spos.astype(np.float64))
     sample = rng.choice(n, 200, replace=False)
-    for i in sample:
-        nb = tree.query_ball_point(spos[i].astype(np.float64), float(h))
-        r2 = ((spos[nb].astype(np.float64) - spos[i].astype(np.float64)) ** 2).sum(1)
-        w = ((h * h - r2[r2 < h * h]) ** 3).sum()
-        assert abs(rho[i] / (d["cd"] * w) - 1.0) < 2e-5
+    w = _sampled_all_pairs_densities(spos, sample, h)
+    assert np.all(np.abs(rho[sample] / (d["cd"] * w) - 1.0) < 2e-5)
 
 
 def test_gather_depth_follows_scene_size_unless_set():
