@@ -22,8 +22,13 @@ Printed JSON line (rank 0):
              SPH library is not part of the reference) on the host cores.
 
 ``--impl reference`` times that CPU implementation as the reference arm.
-``--only adjoint`` runs the differentiable section alone and prints its record
-(a command to profile; it does not print the bench line).
+``--only adjoint`` runs the differentiable section alone and prints its record,
+and ``--only batched`` advances the batched-cube workload for --batch-steps
+steps (default 10) with the default kernel choices (no autotuning, no
+per-scene comparison): commands to profile; they do not print the bench line.
+``--tuning L,D,F,P,W`` sets the headline solver's kernel choices (sf_tuning:
+list mode, density and force block sizes, gather batch, L2 window) instead of
+the defaults.
 """
 from __future__ import annotations
 
@@ -56,6 +61,10 @@ STAGE_BYTES_PER_PARTICLE = {
     "rank_gather": 8 + 8 + 24 + 24,          # read key, cell range; read pos+vel; write pos+vel
 }
 STAGE_BYTES_PER_CELL = {"scan": 4 + 4}  # read the cell histogram, write the cell table
+# Adjoint force pass (k_adj_forces) per particle: read its own step record
+# (x, p | v, 1/rho) 32, adjoint record (apb | avb) 32, (p, 1/rho) 8, rho 4 and
+# list count 4; write (x, rho_bar), (x_bar, k_bar) and v_bar 48.
+ADJ_FORCES_BYTES_PER_PARTICLE = 32 + 32 + 8 + 4 + 4 + 48
 STEP_BYTES_PER_UPDATE = 213  # canonical whole-step figure (hash 20 + sort 16 + reorder 48 + cells 5 + density 20 + force 44 + integrate 60)
 
 # single-scene workloads, batch and adjoint: simplefluid_gb300/workloads/*.json
@@ -181,12 +190,18 @@ def cpu_oracle_rate(pos: np.ndarray, prm, budget_s: float, max_steps: int, warmu
 
 def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
     """Batched cubes: 256 scenes (counts log-uniform in [2000, 65536], seed
-    20171) advanced together (one graph launch per step, autotuned), against
-    stepping each scene on its own context, one scene after another, and
-    against all contexts interleaved on their own streams.  With several ranks
-    the scenes are spread over them (largest first, no communication) and each
-    throughput is all ranks' particle-updates over the slowest rank's time."""
+    20171) advanced together, one graph launch per step, in the configuration
+    the autotuner chooses (grid granularity, and either the five launches'
+    kernel variants or the persistent step's cluster and block size).  Beside
+    it, on the same clock (wall time between synchronisations, the same steps
+    from the same state): the five-launch step and the persistent step with
+    each cluster and block size, every scene stepped on its own context one
+    after another, and all those contexts interleaved on their own streams.
+    With several ranks the scenes are spread over them (largest first, no
+    communication) and each throughput is all ranks' particle-updates over the
+    slowest rank's time."""
     from simplefluid_gb300 import SPHBatch, SPHParameters, SPHSolver, batch_cubes, shard_batch
+    from simplefluid_gb300 import _capi as C
     cfg = configs.load("batched_cubes")
     steps = args.batch_steps if args.batch_steps else cfg["steps"]
     params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))
@@ -194,17 +209,49 @@ def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
     if ws > 1:
         params, counts, pos, _ = shard_batch(params, counts, pos, rank, ws)
     n = int(counts.sum())
+
+    def rate(run) -> float:
+        """All ranks' particle-updates of `steps` steps over the slowest rank's
+        wall-clock time of run() (synchronised on both sides)."""
+        t0 = time.perf_counter()
+        run()
+        t_s, u = aggregate_over_ranks(dist, time.perf_counter() - t0, n * steps)
+        return u / t_s
+
+    variants = {}
     with SPHBatch(params) as b:
         b.setState(counts, pos)
         b.step(3)
         t0 = time.perf_counter()
         tune, K, _ = b.autotune(5)
         tune_s = time.perf_counter() - t0
+        snap = b.getState()
+
+        def timed(t):
+            b.setTuning(t)
+            b.setState(counts, *snap)
+            b.step(3)
+            b.synchronize()
+
+            def run():
+                b.step(steps)
+                b.synchronize()
+            return rate(run)
+
+        chosen = C.sf_tuning()
+        ctypes.memmove(ctypes.byref(chosen), ctypes.byref(tune), ctypes.sizeof(tune))
+        batched = timed(chosen)
+        variants["five_launches"] = timed(C.sf_tuning(C.SF_LIST_TILE, 128, 128, 2, 0, 0, 0))
+        for cl in (4, 8):
+            for bb in (256, 1024):
+                variants[f"persistent_cluster{cl}_block{bb}"] = timed(
+                    C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, cl, bb))
+        # the chosen configuration again, for the device-time figure
+        b.setTuning(chosen)
+        b.setState(counts, *snap)
         b.step(3)
         b.synchronize()
-        ms = b.timedSteps(steps)
-    t_ms, units = aggregate_over_ranks(dist, ms, n * steps)
-    batched = units / (t_ms * 1e-3)
+        dev_ms = b.timedSteps(steps)
     off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     ctxs = []
     try:
@@ -212,27 +259,27 @@ def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
             pp = SPHParameters.from_c(params[s])
             pp.cellsPerH = K
             c = SPHSolver(pp)
-            c.setParticles(pos[off[s]:off[s + 1]])
+            c.setParticles(snap[0][off[s]:off[s + 1]], snap[1][off[s]:off[s + 1]])
             c.makeReady()
             ctxs.append(c)
         for c in ctxs:
             c.step(3)
         for c in ctxs:
             c.synchronize()
-        t0 = time.perf_counter()
-        for c in ctxs:
-            c.step(steps)
-            c.synchronize()
-        t_s, u = aggregate_over_ranks(dist, time.perf_counter() - t0, n * steps)
-        seq = u / t_s
-        t0 = time.perf_counter()
-        for _ in range(steps):
+
+        def sequential():
             for c in ctxs:
-                c.step(1)
-        for c in ctxs:
-            c.synchronize()
-        t_s, u = aggregate_over_ranks(dist, time.perf_counter() - t0, n * steps)
-        rr = u / t_s
+                c.step(steps)
+                c.synchronize()
+
+        def interleaved():
+            for _ in range(steps):
+                for c in ctxs:
+                    c.step(1)
+            for c in ctxs:
+                c.synchronize()
+        seq = rate(sequential)
+        rr = rate(interleaved)
     finally:
         for c in ctxs:
             c.close()
@@ -245,19 +292,46 @@ def measure_batched(args, dist=None, rank: int = 0, ws: int = 1) -> dict:
         for s in sample:
             pp = SPHParameters.from_c(params[s])
             pp.cellsPerH = K
-            rate, st, threads = cpu_oracle_rate(pos[off[s]:off[s + 1]], pp, args.cpu_seconds / 8, 20)
+            rate_s, st, threads = cpu_oracle_rate(pos[off[s]:off[s + 1]], pp, args.cpu_seconds / 8, 20)
             ups += (off[s + 1] - off[s]) * st
-            secs += (off[s + 1] - off[s]) * st / rate
+            secs += (off[s + 1] - off[s]) * st / rate_s
         cpu = {"value": ups / secs, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"scenes {list(sample)} one after another, up to 20 sub-steps each (after 1 warm-up)"}
+    dev_t, units = aggregate_over_ranks(dist, dev_ms, n * steps)
     return {"value": batched, "unit": UNIT, "scenes": total_scenes, "particles": units // steps, "steps": steps,
             "ranks": ws,
             "sequential_value": seq, "ratio_vs_sequential": batched / seq, "interleaved_streams_value": rr,
+            "ratio_vs_interleaved_streams": batched / rr, "variants": variants,
+            "device_time_value": units / (dev_t * 1e-3),
             "cpu_baseline": cpu,
             "autotuned": {"cells_per_h": K, "list_mode": tune.list_mode, "density_block": tune.density_block,
-                          "force_block": tune.force_block, "prefetch": tune.prefetch, "seconds": tune_s},
-            "timing": "batched: CUDA events over the graph-replayed steps (warm L2); sequential and interleaved: "
-                      "wall clock over the same number of steps per scene"}
+                          "force_block": tune.force_block, "prefetch": tune.prefetch,
+                          "batch_cluster": tune.batch_cluster, "batch_block": tune.batch_block,
+                          "seconds": tune_s},
+            "timing": "value, variants, sequential and interleaved: wall clock between synchronisations over the "
+                      "same steps from the same state; device_time_value: CUDA events over the chosen "
+                      "configuration's graph-replayed steps"}
+
+
+def profile_batched(args) -> dict:
+    """The batched-cube workload alone: upload, 3 warm-up steps, then
+    --batch-steps steps (default 10) with the default kernel choices; device
+    time by CUDA events.  A command to profile the batched kernels."""
+    from simplefluid_gb300 import SPHBatch, batch_cubes
+    cfg = configs.load("batched_cubes")
+    steps = args.batch_steps or 10
+    params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))
+    with SPHBatch(params) as b:
+        if args.tuning:
+            from simplefluid_gb300 import _capi as C
+            b.setTuning(C.sf_tuning(*[int(x) for x in args.tuning.split(",")]))
+        b.setState(counts, pos)
+        b.step(3)
+        b.synchronize()
+        ms = b.timedSteps(steps)
+    n = int(counts.sum())
+    return {"scenes": len(params), "particles": n, "steps": steps, "ms_per_step": ms / steps,
+            "value": n * steps / (ms * 1e-3), "unit": UNIT, "tuning": args.tuning}
 
 
 def measure_adjoint(args) -> dict:
@@ -298,10 +372,27 @@ def measure_adjoint(args) -> dict:
             t3 = time.perf_counter()
             cur = ((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3)
             best = cur if best is None or cur[2] < best[2] else best
+        # per-pass device times of the reverse sweep (one segment, CUDA events)
+        npass = lib.sf_adjoint_pass_count()
+        pass_ms = np.zeros(npass, np.float32)
+        seg_steps = ctypes.c_uint32()
+        C.check(lib.sf_adjoint_profile(s.handle, pass_ms.ctypes.data_as(ctypes.c_void_p), npass,
+                                       ctypes.byref(seg_steps)))
+    passes = {lib.sf_adjoint_pass_name(p).decode(): float(pass_ms[p]) / seg_steps.value for p in range(npass)}
+    n = int(pos.shape[0])
+    fbytes = ADJ_FORCES_BYTES_PER_PARTICLE * n
+    avg = passes["adj_forces"]
+    peaks = measured_peaks()
+    achieved = fbytes / (avg * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_adj_forces", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "algorithmic_bytes_per_launch": fbytes, "avg_launch_ms": avg,
+            "peak_source": peaks["source"],
+            "note": "latency-bound at low occupancy: 65,536 particles fill about 13 warps per SM"}
     return {"particles": int(pos.shape[0]), "steps": steps, "ckpt_every": ckpt, "forward_ms": fwd_ms,
             "forward_with_checkpoints_ms": best[0], "loss_ms": best[1], "adjoint_ms": best[2],
             "ratio_adjoint_over_forward": best[2] / fwd_ms, "loss": float(L),
             "dloss_dviscosity": float(dmu), "dloss_dstiffness": float(dk),
+            "passes_ms_per_step": passes, "roofline": roof,
             "timing": "forward: CUDA events over graph-replayed steps; others: wall clock, best of 3, "
                       "adjoint includes the checkpointed forward recompute"}
 
@@ -473,6 +564,9 @@ def run_ours(args, workload):
     pos = scene_positions(prm, prm.scene, configs.load(workload)["seed"])
     n = pos.shape[0]
     solver = SPHSolver(prm)
+    if args.tuning:
+        t = C.sf_tuning(*[int(x) for x in args.tuning.split(",")])
+        C.check(lib.sf_set_tuning(solver.handle, ctypes.byref(t)))
     solver.setParticles(pos)
     solver.makeReady()
     ctx = solver.handle
@@ -606,6 +700,7 @@ def run_ours(args, workload):
                 "path": "sf_set_state(pinned host) + sf_advance_frame + sf_get_state(pinned host)",
                 "state_finite": finite},
         "gpu_launches": kernels_per_step * args.steps,
+        "tuning": args.tuning,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "batched": batched,
@@ -630,13 +725,18 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-other-workloads", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=0, help="default: the batched_cubes configuration's steps")
-    ap.add_argument("--only", choices=["adjoint"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched"], default=None,
                     help="run one section alone and print its record (for profiling); not the bench line")
+    ap.add_argument("--tuning", default=None,
+                    help="kernel choices: list_mode,density_block,force_block,prefetch,l2_window"
+                         "[,batch_cluster,batch_block]")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.only == "adjoint":
         print(json.dumps({"section": "adjoint", **measure_adjoint(args)}), flush=True)
+    elif args.only == "batched":
+        print(json.dumps({"section": "batched", **profile_batched(args)}), flush=True)
     elif args.impl == "reference":
         run_reference(args, args.workload)
     else:

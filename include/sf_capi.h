@@ -270,12 +270,30 @@ SF_API sf_status sf_test_fail_allocation(int64_t after);
 #define SF_LIST_TILE_STAGED 1 /* density pass stages neighbour lists in shared
                                  memory, writes 128-particle tiles             */
 #define SF_LIST_TILE 2        /* direct stores, 128-particle tiles             */
+#define SF_LIST_TILE16 3      /* direct stores of 16-bit entries (the low half
+                                 of the neighbour's index, exact within
+                                 +-32767 sorted places) in 32-particle tiles; a
+                                 tile whose candidate span is wider stores
+                                 32-bit entries instead                        */
 typedef struct sf_tuning {
     int32_t list_mode;     /* SF_LIST_*                                       */
     int32_t density_block; /* threads per block of the density pass: 128, 256 */
     int32_t force_block;   /* threads per block of the force pass: 128, 256   */
     int32_t prefetch;      /* neighbours gathered per batch: 2 or 4           */
-    int32_t reserved[4];   /* must be zero                                    */
+    int32_t l2_window;     /* 1: the force pass's gather records are kept in
+                              L2 with a persisting access-policy window on the
+                              density and force launches; 0: no window       */
+    int32_t batch_cluster; /* batches only.  0: each step is five launches
+                              over all scenes' particles.  2, 4 or 8: each step
+                              is one persistent launch of thread-block
+                              clusters of that many blocks; a cluster takes
+                              whole scenes, largest first, and runs their five
+                              stages between cluster barriers (needs
+                              SF_LIST_TILE; the other fields then do not
+                              apply).  Both compute the same bits.           */
+    int32_t batch_block;   /* threads per block of the persistent step: 256,
+                              512 or 1024 (0 is taken as 256)                */
+    int32_t reserved[1];   /* must be zero                                    */
 } sf_tuning;
 SF_API sf_status sf_get_tuning(const sf_ctx* ctx, sf_tuning* t);
 SF_API sf_status sf_set_tuning(sf_ctx* ctx, const sf_tuning* t);
@@ -359,6 +377,16 @@ SF_API sf_status sf_load_state(sf_ctx* ctx, const char* path, double* sim_time_o
 SF_API sf_status sf_forward(sf_ctx* ctx, uint32_t nsteps, uint32_t ckpt_every);
 SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dloss_dv, float* dloss_dx0,
                             float* dloss_dv0, float* dloss_dviscosity, float* dloss_dstiffness);
+/* Measurement of the adjoint (not in the reference; for benchmarks): after
+ * sf_adjoint, re-runs the reverse sweep of the trajectory's first segment pass
+ * by pass with an event between passes; pass_ms[p] receives pass p's device
+ * time summed over the segment's steps (npasses must equal
+ * sf_adjoint_pass_count()), *steps_out (may be NULL) the number of steps.
+ * It overwrites the adjoint's working buffers: the gradients sf_adjoint
+ * returned are unaffected, and the next sf_adjoint starts afresh. */
+SF_API uint32_t sf_adjoint_pass_count(void);
+SF_API const char* sf_adjoint_pass_name(uint32_t pass);
+SF_API sf_status sf_adjoint_profile(sf_ctx* ctx, float* pass_ms, uint32_t npasses, uint32_t* steps_out);
 /* Loss = sum over res^3 cells of (H_c - target_c)^2, H the cloud-in-cell
  * histogram of the current positions on cell-centred bins over the box,
  * normalised by the particle count (accumulated in 2^-32 fixed point, so it

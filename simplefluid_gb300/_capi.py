@@ -68,13 +68,15 @@ class sf_params(ctypes.Structure):
 SF_LIST_NONE = 0
 SF_LIST_TILE_STAGED = 1
 SF_LIST_TILE = 2
+SF_LIST_TILE16 = 3
 
 
 class sf_tuning(ctypes.Structure):
     """Mirror of ``struct sf_tuning`` (include/sf_capi.h)."""
 
     _fields_ = [("list_mode", c_int32), ("density_block", c_int32), ("force_block", c_int32),
-                ("prefetch", c_int32), ("reserved", c_int32 * 4)]
+                ("prefetch", c_int32), ("l2_window", c_int32), ("batch_cluster", c_int32),
+                ("batch_block", c_int32), ("reserved", c_int32 * 1)]
 
 
 SF_COLOR_UNIFORM = 0
@@ -170,6 +172,9 @@ PROTOTYPES = {
     "sf_stage_count": (c_uint32, []),
     "sf_stage_name": (c_char_p, [c_uint32]),
     "sf_profile_steps": (c_int32, [c_void_p, c_uint32, c_uint64, c_void_p, c_uint32]),
+    "sf_adjoint_pass_count": (c_uint32, []),
+    "sf_adjoint_pass_name": (c_char_p, [c_uint32]),
+    "sf_adjoint_profile": (c_int32, [c_void_p, c_void_p, c_uint32, POINTER(c_uint32)]),
     "sf_get_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_set_tuning": (c_int32, [c_void_p, _P(sf_tuning)]),
     "sf_render_params_default": (c_int32, [_P(sf_render_params)]),

@@ -45,6 +45,7 @@ SOURCES = [
     ("sf_capi_adjoint.cpp", []),
     ("sf_scenes.cpp", []),
     ("sf_noalloc.cu", ["-fmad=false"]),
+    ("sf_batch.cu", ["-fmad=false"]),
 ]
 
 

@@ -429,20 +429,33 @@ __global__ void k_hist_grad(const float4* __restrict__ pos, uint32_t n, SimConst
 SF_INDEX_CHECK_ACCESSOR(index_check_failures_adjoint)
 
 // ------------------------------------------------------------------ launchers
-void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
+const char* const kAdjointPassNames[kAdjointPasses] = {"adj_integrate", "adj_forces", "adj_density"};
+
+void launch_adjoint_pass(uint32_t pass, const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
                          cudaStream_t s) {
     const uint32_t n = st.n;
     if (!n) return;
     const unsigned g = grid_for(n, kAdjBlock);
-    k_adj_integrate<<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.sums, n, c, w.Xb, w.Vb, w.ab, w.xdir, w.vdir);
+    if (pass == 0) {
+        k_adj_integrate<<<g, kAdjBlock, 0, s>>>(st.pos, st.vel, st.pr, st.sums, n, c, w.Xb, w.Vb, w.ab, w.xdir,
+                                                w.vdir);
+        return;
+    }
     const float m6cd = (float)(-6.0 * (double)c.cd);
     with_reach(c.reach, [&](auto R) {
         constexpr int K = decltype(R)::value;
-        k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.pv, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.ab,
-                                                w.xrb, w.xf, w.vf);
-        k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.xrb, w.xdir, w.vdir,
-                                                 w.xf, w.vf, w.ab, w.Xb, w.Vb, partial);
+        if (pass == 1)
+            k_adj_forces<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.pv, st.pr, st.rho, st.cs, st.nbr, st.cnt, n, c, w.ab,
+                                                    w.xrb, w.xf, w.vf);
+        else if (pass == 2)
+            k_adj_density<K><<<g, kAdjBlock, 0, s>>>(st.pos, st.cs, st.nbr, st.cnt, n, c, m6cd, w.xrb, w.xdir, w.vdir,
+                                                     w.xf, w.vf, w.ab, w.Xb, w.Vb, partial);
     });
+}
+
+void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
+                         cudaStream_t s) {
+    for (uint32_t p = 0; p < kAdjointPasses; ++p) launch_adjoint_pass(p, st, c, w, partial, s);
 }
 
 uint32_t adjoint_partial_count(uint32_t n) { return grid_for(n, kAdjBlock); }

@@ -122,7 +122,7 @@ bool is_pinned(const void* p) {
 
 void free_particles(sf::DeviceState& d) {
     void* bufs[] = {d.pos, d.vel, d.pos2, d.vel2, d.pr, d.rho, d.key_slot, d.tmp, d.io, d.accel, d.nbr, d.nbr_count,
-                    d.pv};
+                    d.nbr_wide, d.pv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     d.pos = d.vel = d.pos2 = d.vel2 = d.accel = nullptr;
@@ -133,6 +133,7 @@ void free_particles(sf::DeviceState& d) {
     d.io = nullptr;
     d.nbr = nullptr;
     d.nbr_count = nullptr;
+    d.nbr_wide = nullptr;
     d.pv = nullptr;
     d.cap = 0;
 }
@@ -240,6 +241,7 @@ sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     if (e == cudaSuccess) e = dev_malloc(&d.io, c * 6 * sizeof(float));
     if (e == cudaSuccess) e = dev_malloc(&d.nbr, tiles * sf::kNbCap * sf::kNbTile * sizeof(uint32_t));
     if (e == cudaSuccess) e = dev_malloc(&d.nbr_count, c * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&d.nbr_wide, tiles * (sf::kNbTile / sf::kNbWarpTile));
     if (e == cudaSuccess) e = dev_malloc(&d.pv, c * 2 * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemset(d.nbr_count, 0, c * sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -320,6 +322,8 @@ void enqueue_full_step(sf_ctx* ctx) {
 
 sf_status capture_step(sf_ctx* ctx) {
     drop_graph(ctx);
+    // the gather records' persisting-L2 window (reserved outside the capture)
+    if (ctx->d.tune.l2_window) sf::reserve_persisting_l2((size_t)ctx->d.n * 2 * sizeof(float4));
     cudaGraph_t g = nullptr;
     SF_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_full_step(ctx);

@@ -128,7 +128,9 @@ sf_status build_segment_graph(sf_ctx* ctx, uint32_t len, cudaGraphExec_t* out) {
         ds.nbr_count = r.cnt;
         ds.sums = r.sums;
         ds.pv = r.pv;
-        if (ds.tune.list_mode == SF_LIST_NONE) ds.tune.list_mode = SF_LIST_TILE;
+        // the reverse passes read 32-bit lists
+        if (ds.tune.list_mode != SF_LIST_TILE_STAGED) ds.tune.list_mode = SF_LIST_TILE;
+        ds.tune.l2_window = 0;
         sf::launch_density(ds, ctx->c, st);
         sf::launch_force_integrate(ds, ctx->c, st);
         sf::DeviceState dn = d;
@@ -289,6 +291,7 @@ SF_API sf_status sf_adjoint(sf_ctx* ctx, const float* dloss_dx, const float* dlo
                                 ctx->stream));
         SF_CUDA(cudaGraphLaunch(g, ctx->stream));
     }
+    t->rec_len = std::min(t->nsteps, t->ckpt);  // the records now hold the first segment
     SF_TRY(download_by_id(ctx, dloss_dx0, w.Xb));
     SF_TRY(download_by_id(ctx, dloss_dv0, w.Vb));
     double sc[2];

@@ -21,7 +21,9 @@ sf_status batch_derive(sf_batch* b, int K) {
         const int st = sf::derive_constants(p, &consts[s], &why);
         if (st) return fail(st, std::string("scene ") + std::to_string(s) + ": " + why);
         consts[s].cell_base = (uint32_t)base;
-        base += consts[s].ncells;
+        // scene cell ranges start at multiples of four cells (the persistent
+        // step scans them four cells at a time); the cells between are empty
+        base += (consts[s].ncells + 3) / 4 * 4;
         if (base > kMaxCells) return fail(SF_ERR_GRID_TOO_LARGE, "batch needs more than 2^28 grid cells in total");
     }
     for (auto& p : b->params) p.cells_per_h = K;
@@ -42,6 +44,8 @@ sf_status batch_upload_table(sf_batch* b) {
     b->eng.d.table = b->d_table;
     b->eng.d.scene_off = b->d_off;
     b->eng.d.nscenes = (uint32_t)ns;
+    b->eng.d.scene_order = b->d_order;
+    b->eng.d.scene_queue = b->d_queue;
     return SF_OK;
 }
 
@@ -102,6 +106,9 @@ SF_API sf_status sf_batch_create(const sf_params* per_scene, uint32_t nscenes, s
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->eng.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = dev_malloc(&b->d_off, (nscenes + 1) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_off, 0, (nscenes + 1) * sizeof(uint32_t), b->eng.stream);
+    if (e == cudaSuccess) e = dev_malloc(&b->d_order, nscenes * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dev_malloc(&b->d_queue, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_order, 0, nscenes * sizeof(uint32_t), b->eng.stream);
     if (e != cudaSuccess) {
         sf_batch_destroy(b);
         return cuda_fail(e, "batch creation");
@@ -121,6 +128,8 @@ SF_API sf_status sf_batch_destroy(sf_batch* b) {
     release_ctx(&b->eng);
     if (b->d_table) cudaFree(b->d_table);
     if (b->d_off) cudaFree(b->d_off);
+    if (b->d_order) cudaFree(b->d_order);
+    if (b->d_queue) cudaFree(b->d_queue);
     delete b;
     return SF_OK;
 }
@@ -153,6 +162,11 @@ SF_API sf_status sf_batch_set_state(sf_batch* b, const uint32_t* counts, const f
     SF_TRY(set_device(&b->eng));
     SF_CUDA(cudaStreamSynchronize(b->eng.stream));
     SF_CUDA(cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    // the persistent step's queue order: largest scenes first (ties by index)
+    std::vector<uint32_t> order(ns);
+    for (size_t s = 0; s < ns; ++s) order[s] = (uint32_t)s;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return counts[x] > counts[y]; });
+    SF_CUDA(cudaMemcpy(b->d_order, order.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice));
     b->counts.assign(counts, counts + ns);
     return sf_set_state(&b->eng, pos_xyz, vel_xyz, off[ns]);
 }
@@ -224,9 +238,10 @@ SF_API sf_status sf_batch_set_cells_per_h(sf_batch* b, int32_t cells_per_h) {
 }
 
 // Autotuner: times `trial_steps` graph-replayed steps (after 2 warm-up steps)
-// of every candidate configuration — grid granularity K and the kernel
-// variants — each from the same snapshot of the current state, keeps the
-// fastest, and restores the snapshot.  The chosen K changes the summation
+// of every candidate configuration — grid granularity K, and either the five
+// launches' kernel variants or the persistent step's cluster and block size
+// (its partition of the scenes over the GPU) — each from the same snapshot of
+// the current state, keeps the fastest, and restores the snapshot.  The chosen K changes the summation
 // order (and so the last bits); the kernel variants do not.
 SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning* chosen, int32_t* chosen_cells_per_h,
                                    float* chosen_ms_per_step) {
@@ -243,8 +258,9 @@ SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning*
         sf_tuning t;
     };
     std::vector<Cand> cands;
-    for (int K : {1, 2})
-        for (int mode : {SF_LIST_TILE_STAGED, SF_LIST_TILE})
+    for (int K : {1, 2}) {
+        // five launches per step over all scenes
+        for (int mode : {SF_LIST_TILE_STAGED, SF_LIST_TILE, SF_LIST_TILE16})
             for (int db : {128, 256})
                 for (int fb : {128, 256}) {
                     if (mode == SF_LIST_TILE_STAGED && db != 128) continue;
@@ -255,6 +271,19 @@ SF_API sf_status sf_batch_autotune(sf_batch* b, uint32_t trial_steps, sf_tuning*
                     t.prefetch = 2;
                     cands.push_back({K, t});
                 }
+        // one persistent launch per step, scenes partitioned over clusters
+        for (int cl : {4, 8})
+            for (int bb : {256, 1024}) {
+                sf_tuning t{};
+                t.list_mode = SF_LIST_TILE;
+                t.density_block = 256;
+                t.force_block = 128;
+                t.prefetch = 2;
+                t.batch_cluster = cl;
+                t.batch_block = bb;
+                cands.push_back({K, t});
+            }
+    }
     float best = 0.f;
     size_t best_i = 0;
     for (size_t ci = 0; ci < cands.size(); ++ci) {

@@ -2,6 +2,7 @@
 // the context and batch objects and the helpers the API files share.
 #pragma once
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -34,6 +35,7 @@ struct Trajectory {
     bool valid = false;
     std::vector<float4*> ck;  // per checkpoint: pos then vel (2n float4)
     std::vector<StepRec> rec; // ckpt steps of one segment
+    uint32_t rec_len = 0;     // steps of the segment the records hold (after sf_adjoint: the first)
     float4* snap = nullptr;   // 2n float4: the forward's final state
     float4* stage = nullptr;  // 2n float4: the checkpoint a segment graph starts from
     double2* seg_partial = nullptr;  // ckpt x adjoint_partial_count(n) scalar partials
@@ -95,6 +97,8 @@ struct sf_batch {
     std::vector<uint32_t> counts;  // particles per scene
     sf::SimConst* d_table = nullptr;
     uint32_t* d_off = nullptr;
+    uint32_t* d_order = nullptr;  // scenes in decreasing particle count (the persistent step's queue order)
+    uint32_t* d_queue = nullptr;  // the persistent step's queue counter
 };
 
 namespace sf {

@@ -202,25 +202,39 @@ SF_API sf_status sf_get_tuning(const sf_ctx* ctx, sf_tuning* t) {
     t->density_block = ctx->d.tune.density_block;
     t->force_block = ctx->d.tune.force_block;
     t->prefetch = ctx->d.tune.prefetch;
+    t->l2_window = ctx->d.tune.l2_window;
+    t->batch_cluster = ctx->d.tune.batch_cluster;
+    t->batch_block = ctx->d.tune.batch_block;
     return SF_OK;
 }
 
 SF_API sf_status sf_set_tuning(sf_ctx* ctx, const sf_tuning* t) {
     SF_TRY(need_ctx(ctx));
     if (!t) return fail(SF_ERR_INVALID_ARGUMENT, "null tuning");
-    if (t->list_mode < SF_LIST_NONE || t->list_mode > SF_LIST_TILE)
+    if (t->list_mode < SF_LIST_NONE || t->list_mode > SF_LIST_TILE16)
         return fail(SF_ERR_INVALID_ARGUMENT, "unknown list_mode");
+    if (t->l2_window != 0 && t->l2_window != 1) return fail(SF_ERR_INVALID_ARGUMENT, "l2_window must be 0 or 1");
+    if (t->batch_cluster != 0 && t->batch_cluster != 2 && t->batch_cluster != 4 && t->batch_cluster != 8)
+        return fail(SF_ERR_INVALID_ARGUMENT, "batch_cluster must be 0, 2, 4 or 8");
+    if (t->batch_cluster && !ctx->d.table)
+        return fail(SF_ERR_INVALID_ARGUMENT, "batch_cluster applies to batches only");
+    if (t->batch_cluster && t->list_mode != SF_LIST_TILE)
+        return fail(SF_ERR_INVALID_ARGUMENT, "the persistent batched step records SF_LIST_TILE lists");
+    if (t->batch_block != 0 && t->batch_block != 256 && t->batch_block != 512 && t->batch_block != 1024)
+        return fail(SF_ERR_INVALID_ARGUMENT, "batch_block must be 256, 512 or 1024");
     if ((t->density_block != 128 && t->density_block != 256) || (t->force_block != 128 && t->force_block != 256))
         return fail(SF_ERR_INVALID_ARGUMENT, "block sizes must be 128 or 256");
     if (t->prefetch != 2 && t->prefetch != 4) return fail(SF_ERR_INVALID_ARGUMENT, "prefetch must be 2 or 4");
-    if (t->reserved[0] || t->reserved[1] || t->reserved[2] || t->reserved[3])
-        return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    if (t->reserved[0]) return fail(SF_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
     SF_TRY(set_device(ctx));
     SF_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->d.tune.list_mode = t->list_mode;
     ctx->d.tune.density_block = t->density_block;
     ctx->d.tune.force_block = t->force_block;
     ctx->d.tune.prefetch = t->prefetch;
+    ctx->d.tune.l2_window = t->l2_window;
+    ctx->d.tune.batch_cluster = t->batch_cluster;
+    ctx->d.tune.batch_block = t->batch_block;
     ctx->tune_explicit = true;
     drop_graph(ctx);
     return SF_OK;
@@ -260,6 +274,58 @@ SF_API sf_status sf_profile_steps(sf_ctx* ctx, uint32_t nsteps, uint64_t flush_b
             acc[s] += ms;
         }
     for (uint32_t s = 0; s < sf::kNumStages; ++s) stage_ms[s] = (float)acc[s];
+    return SF_OK;
+}
+
+SF_API uint32_t sf_adjoint_pass_count(void) { return sf::kAdjointPasses; }
+
+SF_API const char* sf_adjoint_pass_name(uint32_t pass) {
+    return pass < sf::kAdjointPasses ? sf::kAdjointPassNames[pass] : "";
+}
+
+SF_API sf_status sf_adjoint_profile(sf_ctx* ctx, float* pass_ms, uint32_t npasses, uint32_t* steps_out) {
+    SF_TRY(need_sorted(ctx));
+    if (!pass_ms || npasses != sf::kAdjointPasses)
+        return fail(SF_ERR_INVALID_ARGUMENT, "pass_ms needs sf_adjoint_pass_count()");
+    sf::Trajectory* t = ctx->traj;
+    if (!t || !t->rec_len || t->rec.size() < t->rec_len || t->n != ctx->d.cap)
+        return fail(SF_ERR_NOT_READY, "no recorded segment: call sf_adjoint first");
+    SF_TRY(set_device(ctx));
+    for (uint32_t p = 0; p < npasses; ++p) pass_ms[p] = 0.f;
+    const uint32_t len = t->rec_len, n = ctx->d.n;
+    const size_t per = (size_t)sf::kAdjointPasses + 1;
+    EventSet ev;
+    SF_CUDA(ev.create(per * len));
+    const uint32_t nb = sf::adjoint_partial_count(n);
+    for (uint32_t k = 0; k < len; ++k) {
+        const uint32_t s = len - 1 - k;  // the reverse sweep's order
+        const sf::StepRec& r = t->rec[s];
+        sf::AdjointStep as;
+        as.n = n;
+        as.pos = r.pos;
+        as.vel = r.vel;
+        as.pr = r.pr;
+        as.rho = r.rho;
+        as.nbr = r.nbr;
+        as.cnt = r.cnt;
+        as.cs = r.cs;
+        as.sums = r.sums;
+        as.pv = r.pv;
+        SF_CUDA(cudaEventRecord(ev.ev[per * k], ctx->stream));
+        for (uint32_t p = 0; p < sf::kAdjointPasses; ++p) {
+            sf::launch_adjoint_pass(p, as, ctx->c, t->w, t->seg_partial + (size_t)s * nb, ctx->stream);
+            SF_CUDA(cudaEventRecord(ev.ev[per * k + p + 1], ctx->stream));
+        }
+    }
+    SF_TRY(check_launch("profiled adjoint"));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t k = 0; k < len; ++k)
+        for (uint32_t p = 0; p < sf::kAdjointPasses; ++p) {
+            float ms = 0.f;
+            SF_CUDA(cudaEventElapsedTime(&ms, ev.ev[per * k + p], ev.ev[per * k + p + 1]));
+            pass_ms[p] += ms;
+        }
+    if (steps_out) *steps_out = len;
     return SF_OK;
 }
 

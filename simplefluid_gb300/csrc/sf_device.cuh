@@ -40,19 +40,32 @@ inline int sm_count() {
 __device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// launch_chained with an access-policy window (null: none): accesses inside
+// the window are cached in L2 as persisting lines, evicted after all others.
 template <typename... KArgs, typename... Args>
-inline void launch_chained(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+inline void launch_chained_window(const cudaAccessPolicyWindow* window, void (*kernel)(KArgs...), unsigned grid,
+                                  unsigned block, cudaStream_t s, Args... args) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    if (window) {
+        attr[1].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[1].val.accessPolicyWindow = *window;
+        cfg.numAttrs = 2;
+    }
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_chained(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    launch_chained_window(nullptr, kernel, grid, block, s, args...);
 }
 
 // Calls f(std::integral_constant<int, K>) for the context's reach K.
@@ -108,6 +121,44 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {  // murmur3 finaliser
 }
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Loads of the per-particle passes.  kNc: through the read-only path, for
+// data that no thread writes during the kernel (every separately launched
+// pass).  !kNc: plain (coherent) global loads, for the persistent batched step,
+// which writes in one stage what its cluster reads in the next (visible
+// across the cluster barrier's release/acquire, which the read-only path does
+// not take part in).  The asm is volatile so that no load moves across a
+// barrier.
+template <bool kNc>
+__device__ __forceinline__ float4 ld_f4(const float4* p) {
+    if constexpr (kNc) {
+        return __ldg(p);
+    } else {
+        float4 v;
+        asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+        return v;
+    }
+}
+template <bool kNc>
+__device__ __forceinline__ float2 ld_f2(const float2* p) {
+    if constexpr (kNc) {
+        return __ldg(p);
+    } else {
+        float2 v;
+        asm volatile("ld.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+        return v;
+    }
+}
+template <bool kNc>
+__device__ __forceinline__ uint32_t ld_u32(const uint32_t* p) {
+    if constexpr (kNc) {
+        return __ldg(p);
+    } else {
+        uint32_t v;
+        asm volatile("ld.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+        return v;
+    }
+}
 
 // Index checks of the checked build (compiled with SF_DEVICE_CHECKS=1; the
 // release build compiles them out).  Every cell-table range end and every
@@ -167,6 +218,7 @@ __device__ __forceinline__ uint32_t checked_end(uint32_t v, uint32_t n) {
 __device__ __forceinline__ uint32_t count_in_cell(uint32_t key, uint32_t* __restrict__ counts,
                                                   uint32_t* __restrict__ tile_sums) {
     const uint32_t slot = atomicAdd(counts + key, 1u);
+    if (!tile_sums) return slot;  // the persistent batched step scans each scene without tile totals
     const unsigned mask = __activemask();
     const uint32_t tile = key / (uint32_t)kScanTile;
     const unsigned peers = __match_any_sync(mask, tile);
@@ -195,7 +247,7 @@ __device__ __forceinline__ float face_gap(float off, int d, float w, float margi
 // path (the force pass's list-overflow rescan).
 // for_candidate_rows calls g(b, e) with the sorted index range [b, e) of each
 // candidate row in that order (ranges of rows out of reach are empty).
-template <int kReach, typename G>
+template <int kReach, bool kNc = true, typename G>
 __device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint32_t* __restrict__ cs, uint32_t n,
                                                    float x, float y, float z, G&& g) {
     const int cx = cell_coord(x, c.bmin[0], c.inv_cell[0], c.n[0]);
@@ -241,27 +293,27 @@ __device__ __forceinline__ void for_candidate_rows(const SimConst& c, const uint
             const int x1 = (kReach > 1 && g2 + ghi2 >= c.prune_h2) ? xb1 : xb;
             const uint32_t* row = plane + dy * (int)n0;
             const bool live = g2 < c.prune_h2;
-            rb[dy + kReach] = live ? checked_end(__ldg(row + x0), n) : 0u;
-            re[dy + kReach] = live ? checked_end(__ldg(row + x1 + 1), n) : 0u;
+            rb[dy + kReach] = live ? checked_end(ld_u32<kNc>(row + x0), n) : 0u;
+            re[dy + kReach] = live ? checked_end(ld_u32<kNc>(row + x1 + 1), n) : 0u;
         }
 #pragma unroll
         for (int dy = 0; dy <= 2 * kReach; ++dy) g(rb[dy], re[dy]);
     }
 }
 
-template <int kReach, typename F>
+template <int kReach, bool kNc = true, typename F>
 __device__ __forceinline__ void for_candidates(const SimConst& c, const uint32_t* __restrict__ cs,
                                                const float4* __restrict__ pos, uint32_t n, float x, float y, float z,
                                                F&& f) {
-    for_candidate_rows<kReach>(c, cs, n, x, y, z, [&](uint32_t b, uint32_t e) {
+    for_candidate_rows<kReach, kNc>(c, cs, n, x, y, z, [&](uint32_t b, uint32_t e) {
         uint32_t j = b;
 #pragma unroll 1
         for (; j + 1 < e; j += 2) {
-            const float4 x0 = ldg4(pos + j), x1 = ldg4(pos + j + 1);
+            const float4 x0 = ld_f4<kNc>(pos + j), x1 = ld_f4<kNc>(pos + j + 1);
             f(j, x0);
             f(j + 1, x1);
         }
-        if (j < e) f(j, ldg4(pos + j));
+        if (j < e) f(j, ld_f4<kNc>(pos + j));
     });
 }
 
@@ -272,9 +324,29 @@ __device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool pred) {
                  "r"(v), "r"((uint32_t)pred));
 }
 
+// The low 16 bits of v at *p where `pred` holds (one predicated store; the
+// store truncates the 32-bit register).
+__device__ __forceinline__ void store16_if(uint16_t* p, uint32_t v, bool pred) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u16 [%0], %1;\n\t}" ::"l"(p),
+                 "r"(v), "r"((uint32_t)pred));
+}
+
+// A 16-bit list entry (zero-extended; read-only path).
+__device__ __forceinline__ uint32_t ld16(const uint16_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.nc.u16 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+// The neighbour index of a 16-bit entry e of particle i: the index within
+// 32767 places of i whose low 16 bits are e.
+__device__ __forceinline__ uint32_t near_index(uint32_t i, uint32_t e) {
+    return i + (uint32_t)(int32_t)(int16_t)(uint16_t)(e - i);
+}
+
 // The candidate walk above with both row loops rolled and the gaps computed
 // per row.
-template <int kReach, typename F>
+template <int kReach, bool kNc = true, typename F>
 __device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const uint32_t* __restrict__ cs,
                                                const float4* __restrict__ pos, uint32_t n, float x, float y, float z,
                                                F&& f) {
@@ -305,18 +377,26 @@ __device__ __forceinline__ void for_candidates_rolled(const SimConst& c, const u
             }
             const int x0 = max(cx + lo, 0), x1 = min(cx + hi, c.n[0] - 1);
             const uint32_t row = c.cell_base + ((uint32_t)zz * (uint32_t)c.n[1] + (uint32_t)yy) * (uint32_t)c.n[0];
-            const uint32_t b = checked_end(__ldg(cs + row + x0), n), e = checked_end(__ldg(cs + row + x1 + 1), n);
+            const uint32_t b = checked_end(ld_u32<kNc>(cs + row + x0), n),
+                           e = checked_end(ld_u32<kNc>(cs + row + x1 + 1), n);
 #pragma unroll 1
-            for (uint32_t j = b; j < e; ++j) f(j, ldg4(pos + j));
+            for (uint32_t j = b; j < e; ++j) f(j, ld_f4<kNc>(pos + j));
         }
     }
 }
 
-// One 32-byte record in one access (sm_100+ 256-bit vector load / store).
+// One 32-byte record in one access (sm_100+ 256-bit vector load / store);
+// kNc as for ld_f4.
+template <bool kNc = true>
 __device__ __forceinline__ void ld8(const float4* __restrict__ p, float4& a, float4& b) {
-    asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-                 : "l"(p));
+    if constexpr (kNc)
+        asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                     : "l"(p));
+    else
+        asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                     : "l"(p));
 }
 __device__ __forceinline__ void st8(float4* __restrict__ p, const float4& a, const float4& b) {
     asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
@@ -358,6 +438,16 @@ __device__ __forceinline__ float pressure_of(const SimConst& c, float rho) {
 // particles, k-major inside a tile, so a warp reads one 128-byte line per k.
 __device__ __forceinline__ size_t nbr_index(uint32_t i, uint32_t k) {
     return ((size_t)(i / kNbTile) * kNbCap + k) * kNbTile + (i % kNbTile);
+}
+// SF_LIST_TILE16 lists are laid out in warp tiles of kNbWarpTile particles,
+// each of which holds either 32-bit entries (nbr_w32_index, in 32-bit units)
+// or 16-bit entries (nbr_w16_index, in 16-bit units: the first half of the
+// tile's 32-bit region), so tiles of either width sit side by side.
+__device__ __forceinline__ size_t nbr_w32_index(uint32_t i, uint32_t k) {
+    return ((size_t)(i / kNbWarpTile) * kNbCap + k) * kNbWarpTile + (i % kNbWarpTile);
+}
+__device__ __forceinline__ size_t nbr_w16_index(uint32_t i, uint32_t k) {
+    return ((size_t)(i / kNbWarpTile) * (2 * kNbCap) + k) * kNbWarpTile + (i % kNbWarpTile);
 }
 
 // Pair terms of particle i with neighbour j (|xi - xj| < h; j == i adds exact

@@ -8,6 +8,8 @@
 // of the same scan that places the particles.  Stability (equal keys keep their
 // previous order) is restored by ranking each particle among its cell's
 // members, which makes the order deterministic and identical to a stable sort.
+#include <mutex>
+
 #include "sf_device.cuh"
 
 namespace sf {
@@ -342,6 +344,65 @@ __global__ void k_check_ids(const uint32_t* __restrict__ seen, uint32_t n, uint3
 
 SF_INDEX_CHECK_ACCESSOR(index_check_failures_grid)
 
+// ---------------------------------------------------------------- persisting L2
+// Persisting-L2 carve-out of the current device for this process, and the
+// largest access-policy window the device takes (bytes; 0 before a
+// reservation or where the device has none).
+struct PersistingL2 {
+    std::mutex m;
+    size_t carve = 0, max_window = 0;
+};
+static PersistingL2* persisting_l2_of_device() {
+    constexpr int kDevices = 64;
+    static PersistingL2 per_device[kDevices];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return (dev >= 0 && dev < kDevices) ? &per_device[dev] : nullptr;
+}
+
+size_t reserve_persisting_l2(size_t want) {
+    PersistingL2* p = persisting_l2_of_device();
+    if (!p) return 0;
+    std::lock_guard<std::mutex> lock(p->m);
+    int dev = 0, maxp = 0, maxw = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess || maxp <= 0 ||
+        maxw <= 0) {
+        cudaGetLastError();
+        return p->carve;
+    }
+    want = std::min(want, (size_t)maxp);
+    if (want > p->carve) {
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+            cudaGetLastError();
+            return p->carve;
+        }
+        p->carve = want;
+    }
+    p->max_window = (size_t)maxw;
+    return p->carve;
+}
+
+bool persisting_window(const void* base, size_t bytes, cudaAccessPolicyWindow* w) {
+    PersistingL2* p = persisting_l2_of_device();
+    if (!p) return false;
+    size_t carve, max_window;
+    {
+        std::lock_guard<std::mutex> lock(p->m);
+        carve = p->carve;
+        max_window = p->max_window;
+    }
+    if (!carve || !base || !bytes) return false;
+    bytes = std::min(bytes, max_window);
+    w->base_ptr = const_cast<void*>(base);
+    w->num_bytes = bytes;
+    w->hitRatio = bytes <= carve ? 1.0f : (float)((double)carve / (double)bytes);
+    w->hitProp = cudaAccessPropertyPersisting;
+    w->missProp = cudaAccessPropertyStreaming;
+    return true;
+}
+
 // ---------------------------------------------------------------- launchers
 void launch_check_state(const DeviceState& d, const SimConst& c, const uint32_t* nbr_count, uint32_t* seen,
                         uint32_t* report, cudaStream_t s) {
@@ -471,6 +532,18 @@ void enqueue_stage(uint32_t stage, DeviceState& d, const SimConst& c, cudaStream
 }
 
 void enqueue_step(DeviceState& d, const SimConst& c, cudaStream_t s) {
+    if (d.table && d.tune.batch_cluster && d.scene_order && d.scene_queue && d.n) {
+        const int block = d.tune.batch_block ? d.tune.batch_block : 256;
+        const int nclusters = batch_persistent_clusters(d.tune.batch_cluster, block, c.reach);
+        if (nclusters > 0) {
+            const BatchStep a{d.pos,       d.vel,         d.pos2,        d.vel2,     d.pr,      d.rho,
+                              d.key_slot,  d.tmp,         d.nbr,         d.nbr_count, d.pv,     d.counts,
+                              d.cell_start, d.table,      d.scene_off,   d.scene_order, d.scene_queue, d.nscenes,
+                              d.n};
+            launch_batch_persistent(a, d.tune.batch_cluster, block, nclusters, c.reach, s);
+            return;
+        }
+    }
     for (uint32_t st = 0; st < kNumStages; ++st) enqueue_stage(st, d, c, s);
 }
 

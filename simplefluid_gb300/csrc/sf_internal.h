@@ -65,6 +65,9 @@ struct Tuning {
     int density_block = 256;       // 128 or 256 threads
     int force_block = 128;         // 128 or 256 threads
     int prefetch = 2;              // neighbours gathered per batch in the force pass: 2 or 4
+    int l2_window = 0;             // 1: persisting L2 window over the gather records
+    int batch_cluster = 0;         // batches: 0 five launches per step; 2, 4, 8 one persistent launch of clusters
+    int batch_block = 0;           // threads per block of the persistent step: 256, 512, 1024 (0: 256)
 };
 
 // Device buffers of one solver context (all owned by the context).
@@ -83,6 +86,7 @@ struct DeviceState {
     float4* accel = nullptr;    // optional acceleration output (inspection)
     uint32_t* nbr = nullptr;       // neighbour lists, tile-major (kNbCap * kNbTile per tile)
     uint32_t* nbr_count = nullptr; // neighbours of each particle (may exceed kNbCap)
+    uint8_t* nbr_wide = nullptr;   // SF_LIST_TILE16: per warp tile (kNbWarpTile particles), 1 where it holds 32-bit entries
     float4* pv = nullptr;          // 2 per particle (32 bytes): (x, y, z, p), (vx, vy, vz, 1/rho)
     float4* sums = nullptr;        // optional: per particle (AP, 0), (AV, 0) of the force pass (adjoint recording)
     FrameState* frame = nullptr;   // adaptive sub-steps read dt here and raise the maxima
@@ -98,19 +102,37 @@ struct DeviceState {
     const SimConst* table = nullptr;
     const uint32_t* scene_off = nullptr;
     uint32_t nscenes = 0;
+    // persistent batched step: scenes in decreasing particle count, and the
+    // queue counter its clusters take scenes from
+    const uint32_t* scene_order = nullptr;
+    uint32_t* scene_queue = nullptr;
 };
 
 // Neighbour lists: up to kNbCap neighbours per particle, in tiles of kNbTile
 // particles (see nbr_index in sf_device.cuh).
 constexpr int kNbTile = 128;
 constexpr int kNbCap = 64;
+constexpr int kNbWarpTile = 32;  // tiles of SF_LIST_TILE16 lists: one warp's particles
 // list emission modes of the density pass
-constexpr int kEmitNone = 0, kEmitStaged = 1, kEmitTile = 2;
+constexpr int kEmitNone = 0, kEmitStaged = 1, kEmitTile = 2, kEmitTile16 = 3;
+// SF_LIST_TILE16: entries hold the neighbour index's low 16 bits, exact when
+// |j - i| <= kNear16 (j = i + (int16_t)(entry - i)).
+constexpr uint32_t kNear16 = 32767;
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kScanBlocksPerSM = 2;  // resident scan blocks per SM (the scan grid's size)
+
+// Persisting L2 (sf_grid.cu).  reserve_persisting_l2(want) grows this
+// process's persisting-L2 carve-out on the current device to `want` bytes
+// (at most the device's maximum; a limit of the process's context, gone with
+// it) and returns it (0 where the device has none); call it outside stream
+// capture.  persisting_window() fills an access-policy window over
+// [base, base + bytes) (cut to the device's largest window, hit ratio scaled
+// to the carve-out) and returns false while no carve-out is reserved.
+size_t reserve_persisting_l2(size_t want);
+bool persisting_window(const void* base, size_t bytes, cudaAccessPolicyWindow* w);
 
 // ---- kernel launchers (sf_grid.cu, sf_density.cu, sf_force.cu); all enqueue on `s`
 void launch_load_aos(const float* pos3, const float* vel3, uint32_t n, float4* pos, float4* vel, cudaStream_t s);
@@ -204,8 +226,14 @@ struct AdjointWork {
     float4* xrb = nullptr;  // per particle (x, y, z, rho_bar): P4's gather record
     double* scalars = nullptr;   // [sum cv_bar, sum k_bar]
 };
-// One step's adjoint; its scalar block partials go to `partial`
-// (adjoint_partial_count(N) entries).
+// The adjoint step's passes: P1 integration and box (adj_integrate), P2 force
+// pair terms and density adjoint (adj_forces), P4 poly6 terms (adj_density).
+constexpr uint32_t kAdjointPasses = 3;
+extern const char* const kAdjointPassNames[kAdjointPasses];
+void launch_adjoint_pass(uint32_t pass, const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
+                         cudaStream_t s);
+// One step's adjoint (its passes in order); its scalar block partials go to
+// `partial` (adjoint_partial_count(N) entries).
 void launch_adjoint_step(const AdjointStep& st, const SimConst& c, AdjointWork& w, double2* partial,
                          cudaStream_t s);
 uint32_t adjoint_partial_count(uint32_t n);
@@ -216,6 +244,36 @@ void launch_histogram_loss(const float4* pos, uint32_t n, const SimConst& c, con
                            const float* target, unsigned long long* hist, float* e2, double* partial, float4* Xb,
                            cudaStream_t s);
 uint32_t histogram_partial_count(uint32_t res);
+
+// ---- persistent batched step (sf_batch.cu) --------------------------------
+struct BatchStep {
+    float4* pos;
+    float4* vel;
+    float4* pos2;
+    float4* vel2;
+    float2* pr;
+    float* rho;
+    uint2* key_slot;
+    uint32_t* tmp;
+    uint32_t* nbr;
+    uint32_t* nbr_count;
+    float4* pv;
+    uint32_t* counts;
+    uint32_t* cell_start;
+    const SimConst* table;
+    const uint32_t* scene_off;
+    const uint32_t* order;
+    uint32_t* queue;
+    uint32_t nscenes;
+    uint32_t n;
+};
+// Clusters of `cluster` blocks (2, 4 or 8) of `block` threads (256, 512 or
+// 1024) of the persistent step that the current device keeps resident at
+// once (0 if it cannot run them).
+int batch_persistent_clusters(int cluster, int block, int reach);
+// One sub-step of every scene: a queue reset and one launch of `nclusters`
+// clusters.  Scene cell ranges must start at multiples of four cells.
+void launch_batch_persistent(const BatchStep& a, int cluster, int block, int nclusters, int reach, cudaStream_t s);
 
 // Density of caller-owned device positions using the library's fixed static
 // scratch (sf_noalloc.cu); no device allocation.

@@ -167,3 +167,31 @@ def test_differentiable_dambreak_65k_200_steps(oracle):
     assert normwise_err(dv0, ov) < 1e-2
     assert dmu == pytest.approx(om, rel=1e-2)
     assert dk == pytest.approx(ok, rel=1e-2)
+
+
+def test_adjoint_profile_times_each_pass_and_leaves_gradients_reproducible():
+    """sf_adjoint_profile needs a finished sf_adjoint, times the first
+    segment's passes, and a following sf_adjoint returns the same bits."""
+    import ctypes
+    lib = C.load()
+    prm, pos, vel, target = case(seed=4)
+    npass = lib.sf_adjoint_pass_count()
+    assert [lib.sf_adjoint_pass_name(p).decode() for p in range(npass)] == ["adj_integrate", "adj_forces",
+                                                                             "adj_density"]
+    ms = np.zeros(npass, np.float32)
+    steps = ctypes.c_uint32()
+    with SPHSolver(prm) as s:
+        s.setParticles(pos, vel)
+        assert lib.sf_adjoint_profile(s.handle, ms.ctypes.data_as(ctypes.c_void_p), npass,
+                                      ctypes.byref(steps)) == C.SF_ERR_NOT_READY
+        s.forward(20, 8)
+        _, dldx = s.lossHistogram(target)
+        first = s.adjoint(dldx)
+        C.check(lib.sf_adjoint_profile(s.handle, ms.ctypes.data_as(ctypes.c_void_p), npass, ctypes.byref(steps)))
+        assert steps.value == 8 and np.all(ms > 0)
+        assert lib.sf_adjoint_profile(s.handle, ms.ctypes.data_as(ctypes.c_void_p), npass - 1,
+                                      None) == C.SF_ERR_INVALID_ARGUMENT
+        again = s.adjoint(dldx)
+    for a, b in zip(first[:2], again[:2]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert first[2:] == again[2:]

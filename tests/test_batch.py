@@ -85,7 +85,8 @@ def test_batch_autotune_restores_state_and_choice_is_valid(oracle):
         t, K, ms = b.autotune(trial_steps=3)
         after = b.getState()
         assert K in (1, 2) and ms > 0
-        assert t.list_mode in (C.SF_LIST_TILE_STAGED, C.SF_LIST_TILE) and t.prefetch == 2
+        assert t.list_mode in (C.SF_LIST_TILE_STAGED, C.SF_LIST_TILE, C.SF_LIST_TILE16) and t.prefetch == 2
+        assert t.batch_cluster in (0, 4, 8)
         assert np.array_equal(before[0].view(np.uint32), after[0].view(np.uint32))
         got = b.getTuning()
         assert bytes(got) == bytes(t)
@@ -138,3 +139,83 @@ def test_batched_cubes_workload_500_steps(oracle):
         opos, ovel = st.original_order()
         assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
         assert np.array_equal(gvel[sl].view(np.uint32), ovel.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K,cluster,block", [(1, 2, 256), (2, 2, 512), (2, 4, 1024), (2, 8, 256), (1, 8, 1024)])
+def test_persistent_batch_step_matches_oracle_and_five_launch_step(oracle, K, cluster, block):
+    """The persistent batched step (one launch of thread-block clusters that
+    take whole scenes, largest first) computes the bits of the five-launch
+    step and of the oracle run on each scene alone; scenes of one and of zero
+    particles included."""
+    params, counts, pos = batch_cubes(9, 7, small_base(cellsPerH=K))
+    # shrink two scenes to one particle and to none (positions of the others kept)
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    keep = np.ones(pos.shape[0], bool)
+    keep[off[2] + 1:off[3]] = False
+    keep[off[4]:off[5]] = False
+    counts = counts.copy()
+    counts[2], counts[4] = 1, 0
+    pos = pos[keep]
+    rng = np.random.default_rng(9)
+    vel = rng.normal(scale=0.1, size=pos.shape).astype(np.float32)
+    out = {}
+    for c in (0, cluster):
+        with SPHBatch(params) as b:
+            b.setTuning(C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, c, block if c else 0))
+            b.setState(counts, pos, vel)
+            b.step(12)
+            out[c] = b.getState()
+            assert b.getTuning().batch_cluster == c
+            rep = b.checkState()
+            assert all(rep[k] == 0 for k in ("non_finite", "outside_box", "unsorted", "cell_table_mismatch", "bad_ids"))
+    for a, bb in zip(out[0], out[cluster]):
+        assert np.array_equal(a.view(np.uint32), bb.view(np.uint32))
+    gpos, gvel = out[cluster]
+    for s, sl in enumerate(_scene_slices(counts)):
+        if counts[s] == 0:
+            continue
+        st = oracle.State(pos[sl], vel[sl])
+        st.step(params[s], 12)
+        st.sort(params[s])
+        opos, ovel = st.original_order()
+        assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
+        assert np.array_equal(gvel[sl].view(np.uint32), ovel.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+def test_persistent_batch_workload_500_steps(oracle):
+    """The batched-cube workload's 500 sub-steps with the persistent step
+    (clusters of 8 blocks of 1024 threads): sampled scenes equal the oracle."""
+    from simplefluid_gb300 import configs
+    cfg = configs.load("batched_cubes")
+    params, counts, pos = batch_cubes(cfg["seed"], cfg["scenes"], configs.params(cfg))
+    with SPHBatch(params) as b:
+        b.setTuning(C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, 8, 1024))
+        b.setState(counts, pos)
+        b.step(cfg["steps"])
+        gpos, gvel = b.getState()
+    slices = _scene_slices(counts)
+    for s in (int(np.argmax(counts)), int(np.argmin(counts)), 100):
+        sl = slices[s]
+        st = oracle.State(pos[sl])
+        st.step(params[s], cfg["steps"])
+        st.sort(params[s])
+        opos, ovel = st.original_order()
+        assert np.array_equal(gpos[sl].view(np.uint32), opos.view(np.uint32)), s
+        assert np.array_equal(gvel[sl].view(np.uint32), ovel.view(np.uint32)), s
+
+
+@pytest.mark.gpu
+def test_persistent_batch_step_rejections():
+    import ctypes
+    params, counts, pos = batch_cubes(3, 3, small_base())
+    with SPHBatch(params) as b:
+        for bad in (C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, 3), C.sf_tuning(C.SF_LIST_TILE16, 256, 128, 2, 0, 4),
+                    C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, 4, 384)):
+            with pytest.raises(C.SFError):
+                b.setTuning(bad)
+    with SPHSolver(SPHParameters.from_c(params[0])) as s:
+        lib = C.load()
+        assert lib.sf_set_tuning(s.handle, ctypes.byref(C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, 4))) == \
+            C.SF_ERR_INVALID_ARGUMENT

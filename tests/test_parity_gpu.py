@@ -431,19 +431,42 @@ def test_tuning_variants_are_bit_identical(oracle):
     st.step(prm.to_c(), 8)
     st.sort(prm.to_c())
     ref_pos, ref_vel = st.original_order()
-    combos = [(m, db, fb, pf) for m in (0, 1, 2) for db in (128, 256) for fb in (128, 256) for pf in (2, 4)
-              if not (m == 0 and pf != 2) and not (m == 1 and db != 128)]
-    for m, db, fb, pf in combos:
-        t = C.sf_tuning(m, db, fb, pf)
+    combos = [(m, db, fb, pf, w) for m in (0, 1, 2, 3) for db in (128, 256) for fb in (128, 256) for pf in (2, 4)
+              for w in (0, 1)
+              if not (m == 0 and pf != 2) and not (m == 1 and db != 128) and not (w == 1 and (db, fb) != (256, 128))]
+    for m, db, fb, pf, w in combos:
+        t = C.sf_tuning(m, db, fb, pf, w)
         gpos, gvel = _tuned_run(prm, pos, t, 8)
-        assert np.array_equal(gpos.view(np.uint32), ref_pos.view(np.uint32)), (m, db, fb, pf)
-        assert np.array_equal(gvel.view(np.uint32), ref_vel.view(np.uint32)), (m, db, fb, pf)
+        assert np.array_equal(gpos.view(np.uint32), ref_pos.view(np.uint32)), (m, db, fb, pf, w)
+        assert np.array_equal(gvel.view(np.uint32), ref_vel.view(np.uint32)), (m, db, fb, pf, w)
+
+
+def test_sixteen_bit_lists_with_wide_tiles(oracle):
+    """SF_LIST_TILE16 on a scene whose candidate spans exceed 32767 sorted
+    places in most warp tiles (a 160 x 120 x 100 lattice: one z-layer of cells
+    holds 19,200 particles, so an inner particle's candidates reach ~38,000
+    places back) but not near the lowest and highest layers: the wide tiles
+    store 32-bit entries, the others 16-bit entries, and the state after 5
+    steps equals the oracle's bit for bit."""
+    r = 0.0025
+    prm = params_16k(particleRadius=r, kernelRadius=4 * r)
+    rng = np.random.default_rng(31)
+    g = np.stack(np.meshgrid(np.arange(160), np.arange(120), np.arange(100), indexing="ij"), -1).reshape(-1, 3)
+    pos = (0.05 + 2 * r * g + rng.uniform(-0.1, 0.1, size=g.shape) * 2 * r).astype(np.float32)
+    gpos, gvel = _tuned_run(prm, pos, C.sf_tuning(C.SF_LIST_TILE16, 256, 128, 2), 5)
+    st = oracle.State(pos)
+    st.step(prm.to_c(), 5)
+    st.sort(prm.to_c())
+    opos, ovel = st.original_order()
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32))
 
 
 def test_tuning_rejects_bad_values(lib):
     import ctypes
     s = SPHSolver(params_16k())
-    for bad in (C.sf_tuning(7, 128, 128, 2), C.sf_tuning(1, 64, 128, 2), C.sf_tuning(1, 128, 128, 3)):
+    for bad in (C.sf_tuning(7, 128, 128, 2), C.sf_tuning(1, 64, 128, 2), C.sf_tuning(1, 128, 128, 3),
+                C.sf_tuning(3, 128, 128, 2, 2), C.sf_tuning(2, 128, 128, 2, 0, 4)):
         assert lib.sf_set_tuning(s.handle, ctypes.byref(bad)) == C.SF_ERR_INVALID_ARGUMENT
     s.close()
 
