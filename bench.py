@@ -28,7 +28,7 @@ steps (default 10) with the default kernel choices (no autotuning, no
 per-scene comparison): commands to profile; they do not print the bench line.
 ``--tuning L,D,F,P,W`` sets the headline solver's kernel choices (sf_tuning:
 list mode, density and force block sizes, gather batch, L2 window) instead of
-the defaults.
+the defaults, and ``--pre-steps N`` measures from the state N sub-steps on.
 """
 from __future__ import annotations
 
@@ -586,7 +586,10 @@ def run_ours(args, workload):
     def max_over_ranks(x: float) -> float:
         return aggregate_over_ranks(dist, x, 0)[0]
 
-    # warm-up; the state after it starts each of the three passes below
+    # later states of the workload (--pre-steps), then the warm-up; the state
+    # after it starts each of the three passes below
+    if args.pre_steps:
+        C.check(lib.sf_step(ctx, args.pre_steps))
     C.check(lib.sf_step(ctx, max(args.warmup, 3)))
     solver.synchronize()
     snap_pos, snap_vel = solver.getState()
@@ -701,6 +704,7 @@ def run_ours(args, workload):
                 "state_finite": finite},
         "gpu_launches": kernels_per_step * args.steps,
         "tuning": args.tuning,
+        "pre_steps": args.pre_steps,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "batched": batched,
@@ -727,6 +731,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=0, help="default: the batched_cubes configuration's steps")
     ap.add_argument("--only", choices=["adjoint", "batched"], default=None,
                     help="run one section alone and print its record (for profiling); not the bench line")
+    ap.add_argument("--pre-steps", type=int, default=0,
+                    help="advance the headline workload this many sub-steps before the warm-up (later states)")
     ap.add_argument("--tuning", default=None,
                     help="kernel choices: list_mode,density_block,force_block,prefetch,l2_window"
                          "[,batch_cluster,batch_block]")

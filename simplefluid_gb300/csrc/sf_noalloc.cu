@@ -21,11 +21,15 @@
 // one stream.
 //
 // Set-up: the first call on a device looks up the scratch's device address
-// with cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.
-#include <atomic>
+// with cudaGetSymbolAddress (with that device current) and caches it with the
+// CUDA context that was current; make that first call before any stream
+// capture.  The address belongs to that context: a call made under another
+// context (after cudaDeviceReset, or with a driver-API context made current on
+// the same device) repeats the set-up for it.
 #include <cstdint>
+#include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "sf_internal.h"
@@ -58,7 +62,32 @@ constexpr uint64_t kNoAllocScratchBytes = kOffTileSums + align256(4ull * kNoAllo
 static __device__ __align__(256) unsigned char g_sf_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
-std::atomic<unsigned char*> g_scratch_addr[kMaxDevices];
+// Per device: the context the cached address was looked up in, and the address.
+struct ScratchAddr {
+    std::mutex m;
+    CUcontext ctx = nullptr;
+    unsigned char* addr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
+
+// The calling thread's current CUDA context (through the driver entry point
+// the runtime hands out, so the library needs no link to the driver library).
+cudaError_t current_context(CUcontext* out) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    static GetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<GetCurrent>(p);
+        else
+            cudaGetLastError();
+    });
+    if (!fn) return cudaErrorNotSupported;
+    return fn(out) == CUDA_SUCCESS ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
 
 __global__ void k_density_to_caller_order(const float4* __restrict__ pos_sorted, const float* __restrict__ rho,
                                           const float2* __restrict__ pr, uint32_t n, float* __restrict__ out_rho,
@@ -73,21 +102,29 @@ __global__ void k_density_to_caller_order(const float4* __restrict__ pos_sorted,
 
 }  // namespace
 
-// Device address of this device's scratch (looked up once per device).
+// Device address of this device's scratch in the current context (looked up
+// once per device and context).
 static cudaError_t noalloc_scratch(unsigned char** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    unsigned char* p = g_scratch_addr[dev].load(std::memory_order_acquire);
-    if (!p) {
+    CUcontext ctx = nullptr;
+    e = current_context(&ctx);
+    if (e != cudaSuccess) return e;
+    ScratchAddr& s = g_scratch_addr[dev];
+    std::lock_guard<std::mutex> lock(s.m);
+    if (!ctx || !s.addr || s.ctx != ctx) {
+        // the look-up also brings up the runtime's context when none is current
         void* addr = nullptr;
         e = cudaGetSymbolAddress(&addr, g_sf_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        p = static_cast<unsigned char*>(addr);
-        g_scratch_addr[dev].store(p, std::memory_order_release);
+        e = current_context(&ctx);
+        if (e != cudaSuccess) return e;
+        s.addr = static_cast<unsigned char*>(addr);
+        s.ctx = ctx;
     }
-    *out = p;
+    *out = s.addr;
     return cudaSuccess;
 }
 

@@ -96,3 +96,42 @@ def test_noalloc_rejects_requests_beyond_the_scratch(lib):
     small_h = params_16k(kernelRadius=0.01, particleRadius=0.0025).to_c()
     st = lib.sf_density_noalloc(ctypes.byref(small_h), ptr, 4, ptr, None, None)
     assert st == C.SF_ERR_CAPACITY and b"262144" in lib.sf_last_error()
+
+
+def test_noalloc_at_the_limits_on_a_caller_stream_without_allocating(lib):
+    """Exactly 65,536 particles on a 64^3 = 262,144-cell grid, queued on the
+    caller's own stream, with the library's allocation hook set to fail the
+    next device allocation: the call still succeeds (it allocates nothing)
+    and matches the allocating entry point."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    h = 0.031  # K = 2 cells per kernel radius: floor(2 / 0.031) = 64 cells per axis
+    prm = params_16k(kernelRadius=h, particleRadius=h / 4)
+    rng = np.random.default_rng(7)
+    g = np.stack(np.meshgrid(np.arange(64), np.arange(32), np.arange(32), indexing="ij"), -1).reshape(-1, 3)
+    sp = 2 * prm.particleRadius
+    pos = (0.005 + g * sp + rng.uniform(-0.1, 0.1, size=g.shape) * sp).astype(np.float32)
+    n = pos.shape[0]
+    assert n == MAX_PARTICLES
+    ref_rho, ref_p = _existing(prm, pos)
+    d_pos = torch.from_numpy(pos).cuda()
+    d_rho = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    d_p = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    cp = prm.to_c()
+    lib.sf_test_fail_allocation(0)
+    try:
+        with torch.cuda.stream(stream):
+            st = lib.sf_density_noalloc(ctypes.byref(cp), ctypes.c_void_p(d_pos.data_ptr()), n,
+                                        ctypes.c_void_p(d_rho.data_ptr()), ctypes.c_void_p(d_p.data_ptr()),
+                                        ctypes.c_void_p(stream.cuda_stream))
+    finally:
+        lib.sf_test_fail_allocation(-1)
+    assert st == C.SF_OK, lib.sf_last_error()
+    stream.synchronize()
+    rho, prs = d_rho.cpu().numpy(), d_p.cpu().numpy()
+    assert np.isfinite(rho).all()
+    assert rel_err(rho, ref_rho) < DENSITY_RTOL
+    assert normwise_err(prs, ref_p) < DENSITY_RTOL
