@@ -21,6 +21,8 @@ from simplefluid_gb300._capi import sf_params
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libsf_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_scenes.so")
+REF_SIM_LIB = os.path.join(HERE, "_ref", "libref_sim.so")
+FRAME_TIME = 0.0333333333  # Source/Simulator.cpp:47
 
 _lib = None
 _ref = None
@@ -77,6 +79,8 @@ def lib() -> ctypes.CDLL:
         l.sfo_frames_f32.argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_uint32, ctypes.c_double, c_uint32,
                                      c_int, POINTER(ctypes.c_double), POINTER(c_uint32), c_void_p, c_uint32]
         l.sfo_max_threads.argtypes = []
+        l.sfo_frame_accounting.argtypes = [c_void_p, c_uint32, ctypes.c_double, ctypes.c_float, c_uint32, c_void_p,
+                                           c_void_p, POINTER(c_uint32)]
         _lib = l
     return _lib
 
@@ -263,6 +267,34 @@ def render(p: sf_params, rp, pos):
     _chk(lib().sfo_render(ctypes.byref(p), ctypes.byref(rp), pos.shape[0], _ptr(pos), _ptr(rgba), _ptr(depth),
                           _ptr(owner)), "render")
     return rgba, depth, owner
+
+
+def frame_accounting(dts, stop_time: float, frame_time: float = FRAME_TIME, cap: int = 100000):
+    """The oracle's frame accounting on given sub-step sizes: (sub-steps per
+    frame, float simulated time after each frame)."""
+    dts = np.ascontiguousarray(dts, np.float32)
+    sub = np.zeros(cap, np.uint32)
+    t = np.zeros(cap, np.float32)
+    nf = c_uint32()
+    _chk(lib().sfo_frame_accounting(_ptr(dts), dts.size, frame_time, stop_time, cap, _ptr(sub), _ptr(t),
+                                    ctypes.byref(nf)), "frame accounting")
+    return sub[:nf.value].copy(), t[:nf.value].copy()
+
+
+def ref_frames(dts, stop_time: float, cap: int = 100000):
+    """The reference's own frame loop (Source/Simulator.cpp, built by
+    build_ref.sh) on given sub-step sizes: (sub-steps per frame, float
+    simulated time after each frame), or None if it is not built."""
+    if not os.path.exists(REF_SIM_LIB):
+        return None
+    r = ctypes.CDLL(REF_SIM_LIB)
+    r.ref_frames.argtypes = [c_void_p, c_uint32, ctypes.c_float, c_uint32, c_void_p, c_void_p, POINTER(c_uint32)]
+    dts = np.ascontiguousarray(dts, np.float32)
+    sub = np.zeros(cap, np.uint32)
+    t = np.zeros(cap, np.float32)
+    nf = c_uint32()
+    _chk(r.ref_frames(_ptr(dts), dts.size, stop_time, cap, _ptr(sub), _ptr(t), ctypes.byref(nf)), "reference frames")
+    return sub[:nf.value].copy(), t[:nf.value].copy()
 
 
 def max_threads() -> int:

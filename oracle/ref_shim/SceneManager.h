@@ -2,7 +2,8 @@
 // Source/SceneManager.cpp compile here without glm, Qt or the Banana library.
 // It declares the same class interface as the reference's
 // Include/SceneManager.h:25-38 and a vector type with glm::vec3's per-component
-// float arithmetic; it contains no scene logic.  Used only by build_ref.sh.
+// float arithmetic; it contains no scene logic.  Used only by build_ref.sh
+// (also by the Simulator shim beside it).
 #pragma once
 #include <cmath>
 #include <memory>
@@ -48,6 +49,8 @@ template <typename T>
 struct SPHParameters {
     T particleRadius = T(0);
     int scene = 0;
+    int numThreads = 0;  // read by Source/Simulator.cpp
+    T stopTime = T(5);
 };
 
 class SceneManager {

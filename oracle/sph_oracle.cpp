@@ -1183,13 +1183,42 @@ int sfo_frames_f32(const sf_params* p, uint32_t n, float* pos, float* vel, uint3
             stp.step(pos, vel, ids);
             if (dts && total < dts_cap) dts[total] = stp.last_dt;
             acc = acc + stp.last_dt;
-            t += (double)stp.last_dt;
             ++it;
             ++total;
         } while ((double)acc < frame_time && it < max_substeps);
+        t += (double)acc;  // the frame's time, summed in float
     }
     if (sim_time) *sim_time = t;
     if (substeps) *substeps = total;
+    return SF_OK;
+}
+
+// The frame accounting of Source/Simulator.cpp:44-56 on a given sequence of
+// sub-step sizes: frames of sub-steps whose sizes, summed in float, reach
+// frame_time, until the simulated time (the frames' float times summed in
+// float) reaches stop_time.  Per frame: the sub-steps taken and the simulated
+// time after it.  Returns SF_ERR_CAPACITY if more than cap frames would run
+// or the sizes run out.
+int sfo_frame_accounting(const float* dts, uint32_t ndts, double frame_time, float stop_time, uint32_t cap,
+                         uint32_t* frame_substeps, float* sim_times, uint32_t* nframes) {
+    if (!dts || !frame_substeps || !sim_times || !nframes) return SF_ERR_INVALID_ARGUMENT;
+    float sim = 0.0f;
+    uint32_t next = 0, nf = 0;
+    while (sim < stop_time) {
+        float acc = 0.0f;
+        uint32_t it = 0;
+        do {
+            if (next >= ndts) return SF_ERR_CAPACITY;
+            acc = acc + dts[next++];
+            ++it;
+        } while ((double)acc < frame_time);
+        sim = sim + acc;
+        if (nf >= cap) return SF_ERR_CAPACITY;
+        frame_substeps[nf] = it;
+        sim_times[nf] = sim;
+        ++nf;
+    }
+    *nframes = nf;
     return SF_OK;
 }
 

@@ -50,8 +50,11 @@ __global__ void k_frame_check(FrameState* __restrict__ fs, double frame_time, ui
     fs->frame_acc = fs->frame_acc + dt;
     fs->iter += 1u;
     fs->substeps += 1u;
-    fs->sim_time += (double)dt;
-    cudaGraphSetConditional(h, ((double)fs->frame_acc < frame_time && fs->iter < max_substeps) ? 1u : 0u);
+    const bool more = (double)fs->frame_acc < frame_time && fs->iter < max_substeps;
+    // a finished frame adds its time, summed in float as the reference's
+    // frameTime is (Source/Simulator.cpp:46-50)
+    if (!more) fs->sim_time += (double)fs->frame_acc;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 }  // namespace

@@ -46,7 +46,7 @@ struct FrameState {
     float frame_acc;     // simulated time of the current frame (float, like frameTime)
     uint32_t iter;       // sub-steps of the current frame
     uint32_t substeps;   // sub-steps since the last reset
-    double sim_time;     // simulated time since the last reset
+    double sim_time;     // simulated time since the last reset: the finished frames' float times, summed
 };
 
 // Fill `c` from `p`; returns SF_OK or an error code (with message in `why`).

@@ -6,7 +6,14 @@
    particle radii.  Small cases are stored whole; all cases carry a SHA-256 of
    the float32 bytes and the particle count.  These pin the scene generators of
    the oracle and of the product.
-2. ``oracle_regression.npz`` — outputs of the CPU oracle (built on x86-64) for a
+2. ``ref_frames.npz`` — the frame accounting of the reference's OWN frame loop
+   (Source/Simulator.cpp's doSimulation, compiled in place by
+   oracle/build_ref.sh into oracle/_ref/libref_sim.so with a solver that
+   returns given sub-step sizes): sub-steps per 1/30 s frame and the float
+   simulated time after each frame, for a fixed step, a seeded varied one, and
+   the adaptive sub-steps the oracle takes on the 16,000-particle dambreak.
+   These pin the frame loops of the oracle and of the product.
+3. ``oracle_regression.npz`` — outputs of the CPU oracle (built on x86-64) for a
    small SPH case: one sort, density, acceleration and 5 full steps.  They are a
    regression record of the oracle itself (not a pin to the reference's solver,
    which is absent) and let a run on another host architecture check that its
@@ -27,7 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
-from oracle import oracle as O  # noqa: E402
+from oracle import oracle as O
+from simplefluid_gb300 import SPHParameters  # noqa: E402
 from simplefluid_gb300._capi import sf_params  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -59,6 +67,23 @@ def small_params() -> sf_params:
     return p
 
 
+def _same(a, b) -> bool:
+    """Equal arrays, floats compared by their bits."""
+    a, b = np.asarray(a), np.asarray(b)
+    if a.dtype != b.dtype or a.shape != b.shape:
+        return False
+    return a.tobytes() == b.tobytes()
+
+
+def save_if_changed(path: str, arrays: dict) -> None:
+    """Write the fixture unless the file already holds exactly these arrays."""
+    if os.path.exists(path):
+        old = np.load(path)
+        if set(old.files) == set(arrays) and all(_same(old[k], v) for k, v in arrays.items()):
+            return
+    np.savez_compressed(path, **arrays)
+
+
 def main() -> None:
     O.build(force=True)
     if O.build_ref(sys.argv[1] if len(sys.argv) > 1 else None) is None:
@@ -73,7 +98,25 @@ def main() -> None:
         out[f"{key}_scene"] = np.array(s, np.int32)
         if pos.shape[0] <= WHOLE_LIMIT:
             out[f"{key}_pos"] = pos
-    np.savez_compressed(os.path.join(HERE, "ref_scenes.npz"), **out)
+    save_if_changed(os.path.join(HERE, "ref_scenes.npz"), out)
+
+    # the reference's frame loop on given sub-step sizes
+    frames = {}
+    rng = np.random.default_rng(20171)
+    adaptive = SPHParameters(particleRadius=0.01, kernelRadius=0.04, adaptiveTimeStep=True, timeStep=5e-3,
+                             stopTime=0.1, scene=16)
+    st = O.State(O.scene(adaptive.to_c(), 16))
+    _, k, adts = st.frames(adaptive.to_c(), 4, record_dts=20000)
+    cases = {"fixed": (np.full(3000, 1e-4, np.float32), 0.2),
+             "varied": (rng.uniform(2e-5, 2e-3, size=4000).astype(np.float32), 0.25),
+             "adaptive16k": (adts[:k].copy(), 0.1)}
+    for name, (dts, stop) in cases.items():
+        sub, times = O.ref_frames(dts, stop)
+        frames[f"{name}_dts"] = dts
+        frames[f"{name}_stop"] = np.array(stop, np.float32)
+        frames[f"{name}_substeps"] = sub
+        frames[f"{name}_sim_times"] = times
+    save_if_changed(os.path.join(HERE, "ref_frames.npz"), frames)
 
     # oracle regression: 10x20x10 block, jitter-free, small box
     p = small_params()
@@ -86,8 +129,9 @@ def main() -> None:
     st2 = O.State(pos)
     st2.step(p, 5)
     p5, v5 = st2.original_order()
-    np.savez_compressed(os.path.join(HERE, "oracle_regression.npz"), pos0=pos, keys=keys, ids=st.ids, cell_start=cs,
-                        rho=rho, prs=prs, acc=acc, nbr_count=cnt, nbr_hash=hsh, pos5=p5, vel5=v5)
+    save_if_changed(os.path.join(HERE, "oracle_regression.npz"),
+                    dict(pos0=pos, keys=keys, ids=st.ids, cell_start=cs, rho=rho, prs=prs, acc=acc, nbr_count=cnt,
+                         nbr_hash=hsh, pos5=p5, vel5=v5))
     print("wrote", sorted(os.listdir(HERE)))
 
 

@@ -90,3 +90,34 @@ def test_adaptive_rejected_for_gradients_and_batches():
             s.forward(4, 2)
     with pytest.raises(C.SFError):
         SPHBatch([prm.to_c()])
+
+
+def test_frame_loop_matches_the_reference_frame_loop():
+    """On the adaptive 16,000-particle dambreak from rest, the device frame loop
+    (one graph launch per frame) and the headless Simulator report the
+    reference's own frame loop (Source/Simulator.cpp run on the same sub-step
+    sizes, tests/golden/ref_frames.npz): sub-steps per 1/30 s frame and the float
+    simulated time after each frame, bit for bit."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_frames.npz"))
+    want_sub, want_t = g["adaptive16k_substeps"], g["adaptive16k_sim_times"]
+    prm = params_16k(adaptiveTimeStep=True, timeStep=5e-3, stopTime=0.1)
+    pos = scene_positions(prm, C.SF_SCENE_DAMBREAK_16K)
+    subs, times = [], []
+    with SPHSolver(prm) as s:
+        s.setParticles(pos)
+        sim_t = np.float32(0.0)
+        while sim_t < np.float32(prm.stopTime):
+            t, k = s.advanceFrames(1)
+            sim_t = np.float32(sim_t + np.float32(t))
+            subs.append(k)
+            times.append(sim_t)
+    assert np.array_equal(np.array(subs, np.uint32), want_sub)
+    assert np.array_equal(np.array(times, np.float32).view(np.uint32), want_t.view(np.uint32))
+    sim = Simulator(prm)
+    reported = []
+    sim.setupScene()
+    sim.systemTimeChanged = lambda t: reported.append(np.float32(t))
+    sim.startSimulation()
+    sim.wait()
+    assert np.array_equal(np.array(reported, np.float32).view(np.uint32), want_t.view(np.uint32))

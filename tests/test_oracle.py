@@ -192,3 +192,40 @@ def test_boundary_clamp_and_restitution(oracle):
 def test_params_default_is_16k_workload():
     p = params_16k()
     assert p.kernelRadius == 4 * p.particleRadius
+
+
+def test_frame_accounting_matches_the_reference_frame_loop(oracle):
+    """The oracle's frame accounting (sub-steps summed in float to 1/30 s frames,
+    frame times summed in float to the simulated time) reports what the
+    reference's own frame loop (Source/Simulator.cpp, run on the same sub-step
+    sizes; tests/golden/ref_frames.npz) reports: sub-steps per frame and the
+    simulated time after each frame, bit for bit."""
+    g = np.load(os.path.join(GOLD, "ref_frames.npz"))
+    for case in ("fixed", "varied", "adaptive16k"):
+        sub, times = oracle.frame_accounting(g[case + "_dts"], float(g[case + "_stop"]))
+        assert np.array_equal(sub, g[case + "_substeps"]), case
+        assert np.array_equal(times.view(np.uint32), g[case + "_sim_times"].view(np.uint32)), case
+
+
+def test_frame_accounting_against_the_reference_live(oracle):
+    """Where the reference's frame loop is built here, compare on fresh sizes too."""
+    rng = np.random.default_rng(5)
+    dts = rng.uniform(1e-5, 4e-3, size=20000).astype(np.float32)
+    ref = oracle.ref_frames(dts, 1.0)
+    if ref is None:
+        pytest.skip("the reference's frame loop is not built on this machine")
+    sub, times = oracle.frame_accounting(dts, 1.0)
+    assert np.array_equal(sub, ref[0]) and np.array_equal(times.view(np.uint32), ref[1].view(np.uint32))
+
+
+def test_oracle_adaptive_substeps_reproduce_the_frames_fixture(oracle):
+    """The oracle's adaptive sub-steps on the 16,000-particle dambreak from rest
+    are the sizes the frames fixture was made from (on this host's build)."""
+    from simplefluid_gb300 import SPHParameters
+    g = np.load(os.path.join(GOLD, "ref_frames.npz"))
+    p = SPHParameters(particleRadius=0.01, kernelRadius=0.04, adaptiveTimeStep=True, timeStep=5e-3, stopTime=0.1,
+                      scene=16).to_c()
+    st = oracle.State(oracle.scene(p, 16))
+    _, k, dts = st.frames(p, 4, record_dts=20000)
+    n = g["adaptive16k_dts"].size
+    assert k >= n and np.array_equal(dts[:n].view(np.uint32), g["adaptive16k_dts"].view(np.uint32))
