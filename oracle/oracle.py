@@ -4,8 +4,10 @@ Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use
 it, as the checker.  The product package never imports this module.
 
 Parity with the reference's solver library (Banana SPHSolver, absent from the
-reference tree) is unpinned; the scene generators are pinned against the
-reference's own Source/SceneManager.cpp compiled by build_ref.sh.
+reference tree) is unpinned; the scene generators, the frame loop and the
+particle shaders' arithmetic are pinned against the reference's own
+Source/SceneManager.cpp, Source/Simulator.cpp and Shaders/particle.*.glsl
+compiled by build_ref.sh.
 """
 from __future__ import annotations
 
@@ -22,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libsf_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_scenes.so")
 REF_SIM_LIB = os.path.join(HERE, "_ref", "libref_sim.so")
+REF_SHADER_LIB = os.path.join(HERE, "_ref", "libref_shader.so")
 FRAME_TIME = 0.0333333333  # Source/Simulator.cpp:47
 
 _lib = None
@@ -76,6 +79,10 @@ def lib() -> ctypes.CDLL:
             getattr(l, f"sfo_loss_{sfx}").argtypes = [P, c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
                                                       c_void_p]
         l.sfo_render.argtypes = [P, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.sfo_render_camera.argtypes = [P, c_void_p, c_void_p, c_void_p, POINTER(ctypes.c_float),
+                                        POINTER(ctypes.c_float)]
+        l.sfo_particle_vertex.argtypes = [P, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.sfo_particle_fragment.argtypes = [P, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         l.sfo_frames_f32.argtypes = [P, c_uint32, c_void_p, c_void_p, c_void_p, c_uint32, ctypes.c_double, c_uint32,
                                      c_int, POINTER(ctypes.c_double), POINTER(c_uint32), c_void_p, c_uint32]
         l.sfo_max_threads.argtypes = []
@@ -267,6 +274,106 @@ def render(p: sf_params, rp, pos):
     _chk(lib().sfo_render(ctypes.byref(p), ctypes.byref(rp), pos.shape[0], _ptr(pos), _ptr(rgba), _ptr(depth),
                           _ptr(owner)), "render")
     return rgba, depth, owner
+
+
+def render_camera(p: sf_params, rp):
+    """The renderer's camera: (view matrix (16,), projection matrix (16,),
+    column-major, point scale, point radius)."""
+    V = np.zeros(16, np.float32)
+    Pm = np.zeros(16, np.float32)
+    scale, radius = ctypes.c_float(), ctypes.c_float()
+    _chk(lib().sfo_render_camera(ctypes.byref(p), ctypes.byref(rp), _ptr(V), _ptr(Pm), ctypes.byref(scale),
+                                 ctypes.byref(radius)), "render camera")
+    return V, Pm, scale.value, radius.value
+
+
+def particle_vertex(p: sf_params, rp, pos):
+    """The renderer's vertex stage: (eye-space centres (n,3), point sizes (n,),
+    clip positions (n,4))."""
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    eye = np.zeros((n, 3), np.float32)
+    size = np.zeros(n, np.float32)
+    clip = np.zeros((n, 4), np.float32)
+    _chk(lib().sfo_particle_vertex(ctypes.byref(p), ctypes.byref(rp), n, _ptr(pos), _ptr(eye), _ptr(size),
+                                   _ptr(clip)), "particle vertex")
+    return eye, size, clip
+
+
+def particle_fragment(p: sf_params, rp, eye, uv, color=None):
+    """The renderer's fragment stage: (rgba (n,4), discarded (n,) bool); rgba
+    is NaN where the fragment was discarded.  color None = the material's
+    diffuse colour."""
+    eye = np.ascontiguousarray(eye, np.float32).reshape(-1, 3)
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    n = eye.shape[0]
+    col = None if color is None else np.ascontiguousarray(color, np.float32).reshape(n, 3)
+    rgba = np.full((n, 4), np.nan, np.float32)
+    disc = np.zeros(n, np.uint8)
+    _chk(lib().sfo_particle_fragment(ctypes.byref(p), ctypes.byref(rp), n, _ptr(eye), _ptr(uv), _ptr(col),
+                                     _ptr(rgba), _ptr(disc)), "particle fragment")
+    return rgba, disc.astype(bool)
+
+
+def _ref_shader():
+    if not os.path.exists(REF_SHADER_LIB):
+        return None
+    r = ctypes.CDLL(REF_SHADER_LIB)
+    F = ctypes.c_float
+    r.ref_particle_vs.argtypes = [c_void_p, c_void_p, F, F, c_void_p, c_void_p, c_void_p, c_void_p]
+    r.ref_particle_fs.argtypes = [c_void_p, c_int, c_void_p, F, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
+    r.ref_particle_fs.restype = c_int
+    return r
+
+
+def ref_particle_vertex(V, Pm, radius: float, scale: float, pos):
+    """The reference's own vertex shader (Shaders/particle.vs.glsl, built by
+    build_ref.sh) per particle: same outputs as particle_vertex, or None if
+    it is not built."""
+    r = _ref_shader()
+    if r is None:
+        return None
+    V = np.ascontiguousarray(V, np.float32)
+    Pm = np.ascontiguousarray(Pm, np.float32)
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    eye = np.zeros((n, 3), np.float32)
+    size = np.zeros(n, np.float32)
+    clip = np.zeros((n, 4), np.float32)
+    for i in range(n):
+        r.ref_particle_vs(_ptr(V), _ptr(Pm), radius, scale, _ptr(pos[i]), _ptr(eye[i]), _ptr(size[i:i + 1]),
+                          _ptr(clip[i]))
+    return eye, size, clip
+
+
+def ref_particle_fragment(rp, radius: float, eye, uv, color=None):
+    """The reference's own fragment shader (Shaders/particle.fs.glsl, built by
+    build_ref.sh) per fragment, with rp's lights and material: same outputs as
+    particle_fragment, or None if it is not built."""
+    r = _ref_shader()
+    if r is None:
+        return None
+    lights = np.zeros((8, 16), np.float32)
+    for l in range(8):
+        lights[l, 0:4] = rp.light_ambient[l][:]
+        lights[l, 4:8] = rp.light_diffuse[l][:]
+        lights[l, 8:12] = rp.light_specular[l][:]
+        lights[l, 12:16] = rp.light_position[l][:]
+    mat = np.zeros(13, np.float32)
+    mat[0:4] = rp.mat_ambient[:]
+    mat[4:8] = rp.mat_diffuse[:]
+    mat[8:12] = rp.mat_specular[:]
+    mat[12] = rp.mat_shininess
+    eye = np.ascontiguousarray(eye, np.float32).reshape(-1, 3)
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    n = eye.shape[0]
+    col = np.zeros((n, 3), np.float32) if color is None else np.ascontiguousarray(color, np.float32).reshape(n, 3)
+    rgba = np.full((n, 4), np.nan, np.float32)
+    disc = np.zeros(n, bool)
+    for k in range(n):
+        disc[k] = bool(r.ref_particle_fs(_ptr(lights), rp.num_lights, _ptr(mat), radius, 0 if color is None else 1,
+                                         _ptr(col[k]), _ptr(eye[k]), _ptr(uv[k]), _ptr(rgba[k])))
+    return rgba, disc
 
 
 def frame_accounting(dts, stop_time: float, frame_time: float = FRAME_TIME, cap: int = 100000):

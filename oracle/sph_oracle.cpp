@@ -748,12 +748,20 @@ struct SplatO {
     float e[3], x0, y0, size, depth;
 };
 
+// The vertex stage (Shaders/particle.vs.glsl:24-35): eye-space centre e,
+// point size and clip position c of one particle.  The view matrix's bottom
+// row is (0, 0, 0, 1), so the eye coordinate's w is exactly 1 and the
+// projection's last column is added as is.
+void vertex_o(const RCo& rc, const float* p, float* e, float& size, float* c) {
+    for (int r = 0; r < 3; ++r) e[r] = ((rc.V[r] * p[0] + rc.V[4 + r] * p[1]) + rc.V[8 + r] * p[2]) + rc.V[12 + r];
+    const float dist = std::sqrt((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]);
+    size = rc.radius * (rc.scale / dist);
+    for (int r = 0; r < 4; ++r) c[r] = ((rc.P[r] * e[0] + rc.P[4 + r] * e[1]) + rc.P[8 + r] * e[2]) + rc.P[12 + r];
+}
+
 bool splat_o(const RCo& rc, const float* p, SplatO& s) {
-    for (int r = 0; r < 3; ++r) s.e[r] = ((rc.V[r] * p[0] + rc.V[4 + r] * p[1]) + rc.V[8 + r] * p[2]) + rc.V[12 + r];
-    const float dist = std::sqrt((s.e[0] * s.e[0] + s.e[1] * s.e[1]) + s.e[2] * s.e[2]);
-    s.size = rc.radius * (rc.scale / dist);
     float c[4];
-    for (int r = 0; r < 4; ++r) c[r] = ((rc.P[r] * s.e[0] + rc.P[4 + r] * s.e[1]) + rc.P[8 + r] * s.e[2]) + rc.P[12 + r];
+    vertex_o(rc, p, s.e, s.size, c);
     if (!(c[3] > 0.f)) return false;
     if (c[0] < -c[3] || c[0] > c[3] || c[1] < -c[3] || c[1] > c[3] || c[2] < -c[3] || c[2] > c[3]) return false;
     const float nx = c[0] / c[3], ny = c[1] / c[3], nz = c[2] / c[3];
@@ -765,17 +773,57 @@ bool splat_o(const RCo& rc, const float* p, SplatO& s) {
     return true;
 }
 
-float disc_o(const SplatO& s, int px, int row, float& nx, float& ny) {
-    const float u = (((float)px + 0.5f) - s.x0) / s.size;
-    const float v = (((float)row + 0.5f) - s.y0) / s.size;
+// gl_PointCoord (u, v) to the sprite normal's x and y and their squared
+// length (Shaders/particle.fs.glsl:67-68).
+float coord_normal_o(float u, float v, float& nx, float& ny) {
     nx = u * 2.0f + -1.0f;
     ny = v * -2.0f + 1.0f;
     return nx * nx + ny * ny;
 }
 
+// Pixel (px, row) of a splat: its point coordinate, then the normal.
+float disc_o(const SplatO& s, int px, int row, float& nx, float& ny) {
+    const float u = (((float)px + 0.5f) - s.x0) / s.size;
+    const float v = (((float)row + 0.5f) - s.y0) / s.size;
+    return coord_normal_o(u, v, nx, ny);
+}
+
 void normalize_o(float* v) {
     const float len = std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
     for (int a = 0; a < 3; ++a) v[a] = v[a] / len;
+}
+
+// The fragment stage from the normal on (Shaders/particle.fs.glsl:46-59 and
+// 70-83) for a fragment that was not discarded: Blinn-Phong per light,
+// summed in light order; surf is the surface colour (the particle's colour,
+// or the material's diffuse colour).
+void shade_o(const sf_render_params* rp, float radius, const float* e, float nx, float ny, float mag,
+             const float* surf, float* out) {
+    const float nrm[3] = {nx, ny, std::sqrt(1.0f - mag)};
+    float view[3] = {e[0], e[1], e[2]};
+    normalize_o(view);
+    const float frag[3] = {e[0] + nrm[0] * radius, e[1] + nrm[1] * radius, e[2] + nrm[2] * radius};
+    float shade[3] = {0, 0, 0};
+    for (int l = 0; l < rp->num_lights; ++l) {
+        float ld[3] = {rp->light_position[l][0] - frag[0], rp->light_position[l][1] - frag[1],
+                       rp->light_position[l][2] - frag[2]};
+        normalize_o(ld);
+        float hd[3] = {ld[0] - view[0], ld[1] - view[1], ld[2] - view[2]};
+        normalize_o(hd);
+        const float diff = std::max((nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2], 0.f);
+        const float spec =
+            std::pow(std::max((hd[0] * nrm[0] + hd[1] * nrm[1]) + hd[2] * nrm[2], 0.f), rp->mat_shininess);
+        for (int a = 0; a < 3; ++a) {
+            const float amb = rp->light_ambient[l][a] * rp->mat_ambient[a];
+            const float dif = (rp->light_diffuse[l][a] * diff) * surf[a];
+            const float spc = (rp->light_specular[l][a] * spec) * rp->mat_specular[a];
+            shade[a] += (amb + dif) + spc;
+        }
+    }
+    out[0] = shade[0];
+    out[1] = shade[1];
+    out[2] = shade[2];
+    out[3] = 1.0f;
 }
 
 void color_o(const sf_render_params* rp, uint32_t id, uint32_t n, float* col) {
@@ -1123,35 +1171,11 @@ int sfo_render(const sf_params* p, const sf_render_params* rp, uint32_t n, const
             SplatO s;
             splat_o(rc, pos3 + 3 * (size_t)id, s);
             const int px = (int)(pix % (size_t)rc.W), row = (int)(pix / (size_t)rc.W);
-            float nrm[3];
-            const float mag = disc_o(s, px, row, nrm[0], nrm[1]);
-            nrm[2] = std::sqrt(1.0f - mag);
-            float view[3] = {s.e[0], s.e[1], s.e[2]};
-            normalize_o(view);
-            const float frag[3] = {s.e[0] + nrm[0] * rc.radius, s.e[1] + nrm[1] * rc.radius, s.e[2] + nrm[2] * rc.radius};
+            float nx, ny;
+            const float mag = disc_o(s, px, row, nx, ny);
             float surf[3] = {rp->mat_diffuse[0], rp->mat_diffuse[1], rp->mat_diffuse[2]};
             if (rp->color_mode != SF_COLOR_UNIFORM) color_o(rp, id, n, surf);
-            float shade[3] = {0, 0, 0};
-            for (int l = 0; l < rp->num_lights; ++l) {
-                float ld[3] = {rp->light_position[l][0] - frag[0], rp->light_position[l][1] - frag[1],
-                               rp->light_position[l][2] - frag[2]};
-                normalize_o(ld);
-                float hd[3] = {ld[0] - view[0], ld[1] - view[1], ld[2] - view[2]};
-                normalize_o(hd);
-                const float diff = std::max((nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2], 0.f);
-                const float spec = std::pow(std::max((hd[0] * nrm[0] + hd[1] * nrm[1]) + hd[2] * nrm[2], 0.f),
-                                            rp->mat_shininess);
-                for (int a = 0; a < 3; ++a) {
-                    const float amb = rp->light_ambient[l][a] * rp->mat_ambient[a];
-                    const float dif = (rp->light_diffuse[l][a] * diff) * surf[a];
-                    const float spc = (rp->light_specular[l][a] * spec) * rp->mat_specular[a];
-                    shade[a] += (amb + dif) + spc;
-                }
-            }
-            out[0] = shade[0];
-            out[1] = shade[1];
-            out[2] = shade[2];
-            out[3] = 1.0f;
+            shade_o(rp, rc.radius, s.e, nx, ny, mag, surf, out);
             dep = s.depth;
             own = id;
         }
@@ -1159,6 +1183,50 @@ int sfo_render(const sf_params* p, const sf_render_params* rp, uint32_t n, const
             for (int a = 0; a < 4; ++a) rgba[4 * pix + a] = out[a];
         if (depth) depth[pix] = dep;
         if (owner) owner[pix] = own;
+    }
+    return SF_OK;
+}
+
+// The render's camera: the view and projection matrices (column-major), the
+// point scale (Source/FluidRenderWidget.cpp:66) and the point radius.
+int sfo_render_camera(const sf_params* p, const sf_render_params* rp, float* V16, float* P16, float* scale,
+                      float* radius) {
+    if (!p || !rp || rp->width <= 0 || rp->height <= 0) return SF_ERR_INVALID_ARGUMENT;
+    const RCo rc = render_const(rp, p->particle_radius);
+    for (int k = 0; k < 16; ++k) {
+        if (V16) V16[k] = rc.V[k];
+        if (P16) P16[k] = rc.P[k];
+    }
+    if (scale) *scale = rc.scale;
+    if (radius) *radius = rc.radius;
+    return SF_OK;
+}
+
+// The vertex stage for n particles: eye-space centres (n x 3), point sizes
+// and clip positions (n x 4).
+int sfo_particle_vertex(const sf_params* p, const sf_render_params* rp, uint32_t n, const float* pos3, float* eye3,
+                        float* size, float* clip4) {
+    if (!p || !rp || !pos3 || rp->width <= 0 || rp->height <= 0) return SF_ERR_INVALID_ARGUMENT;
+    const RCo rc = render_const(rp, p->particle_radius);
+    for (uint32_t i = 0; i < n; ++i) vertex_o(rc, pos3 + 3 * (size_t)i, eye3 + 3 * (size_t)i, size[i], clip4 + 4 * (size_t)i);
+    return SF_OK;
+}
+
+// The fragment stage for n fragments: sprite centre in eye space (n x 3),
+// point coordinate (n x 2) and surface colour (n x 3; NULL = the material's
+// diffuse colour).  discarded[k] = 1 where the coordinate falls outside the
+// disc (rgba then untouched), else 0 with rgba (n x 4) written.
+int sfo_particle_fragment(const sf_params* p, const sf_render_params* rp, uint32_t n, const float* eye3,
+                          const float* uv2, const float* color3, float* rgba4, uint8_t* discarded) {
+    if (!p || !rp || !eye3 || !uv2 || !rgba4 || !discarded) return SF_ERR_INVALID_ARGUMENT;
+    const float radius = rp->point_radius > 0.f ? rp->point_radius : p->particle_radius;
+    for (uint32_t k = 0; k < n; ++k) {
+        float nx, ny;
+        const float mag = coord_normal_o(uv2[2 * (size_t)k], uv2[2 * (size_t)k + 1], nx, ny);
+        discarded[k] = mag > 1.0f ? 1 : 0;
+        if (discarded[k]) continue;
+        const float* surf = color3 ? color3 + 3 * (size_t)k : rp->mat_diffuse;
+        shade_o(rp, radius, eye3 + 3 * (size_t)k, nx, ny, mag, surf, rgba4 + 4 * (size_t)k);
     }
     return SF_OK;
 }

@@ -13,7 +13,16 @@
    simulated time after each frame, for a fixed step, a seeded varied one, and
    the adaptive sub-steps the oracle takes on the 16,000-particle dambreak.
    These pin the frame loops of the oracle and of the product.
-3. ``oracle_regression.npz`` — outputs of the CPU oracle (built on x86-64) for a
+3. ``ref_shader.npz`` — outputs of the reference's OWN particle shaders
+   (Shaders/particle.vs.glsl and particle.fs.glsl, compiled as C++ by
+   oracle/build_ref.sh into oracle/_ref/libref_shader.so) for two render
+   settings (the viewer's defaults, and eight seeded lights with another
+   camera and material): per seeded particle the eye-space centre, point size
+   and clip position; per seeded fragment (point coordinate, sprite centre,
+   colour) the discard decision and the colour, for uniform and per-particle
+   colours.  The render settings are stored as the bytes of sf_render_params.
+   These pin the oracle's restatement of the shader arithmetic.
+4. ``oracle_regression.npz`` — outputs of the CPU oracle (built on x86-64) for a
    small SPH case: one sort, density, acceleration and 5 full steps.  They are a
    regression record of the oracle itself (not a pin to the reference's solver,
    which is absent) and let a run on another host architecture check that its
@@ -35,7 +44,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O
-from simplefluid_gb300 import SPHParameters  # noqa: E402
+from simplefluid_gb300 import SPHParameters, render_params  # noqa: E402
 from simplefluid_gb300._capi import sf_params  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -84,6 +93,47 @@ def save_if_changed(path: str, arrays: dict) -> None:
     np.savez_compressed(path, **arrays)
 
 
+# point coordinates at the disc's centre, on its rim (kept: the shader
+# discards only where the squared length exceeds 1) and at the corners
+EDGE_UV = np.array([[0.5, 0.5], [0.5, 0.0], [0.0, 0.5], [1.0, 0.5], [0.5, 1.0], [0.0, 0.0], [1.0, 1.0],
+                    [0.25, 0.25]], np.float32)
+
+
+def shader_cases() -> dict:
+    """The reference's particle shaders on seeded particles and fragments."""
+    rng = np.random.default_rng(4101)
+    viewer = render_params()
+    lights8 = render_params(width=640, height=480, eye=(2.5, 1.5, -2.0), focus=(0.1, 0.0, 0.2), fovy_deg=40.0,
+                            point_radius=0.03, num_lights=8, mat_shininess=64.0)
+    for l in range(8):
+        lights8.light_position[l][:] = [*rng.uniform(-20, 20, 3), 1.0]
+        lights8.light_ambient[l][:] = [*rng.uniform(0, 0.2, 3), 1.0]
+        lights8.light_diffuse[l][:] = [*rng.uniform(0, 1, 3), 1.0]
+        lights8.light_specular[l][:] = [*rng.uniform(0, 1, 3), 1.0]
+    lights8.mat_ambient[:] = [*rng.uniform(0, 1, 3), 1.0]
+    lights8.mat_diffuse[:] = [*rng.uniform(0, 1, 3), 1.0]
+    lights8.mat_specular[:] = [*rng.uniform(0, 1, 3), 1.0]
+    out = {}
+    for name, rp, radius in (("viewer", viewer, 0.01), ("lights8", lights8, 0.02)):
+        p = SPHParameters(particleRadius=radius).to_c()
+        V, Pm, scale, rad = O.render_camera(p, rp)
+        pos = rng.uniform(-1.0, 1.0, size=(1024, 3)).astype(np.float32)
+        eye, size, clip = O.ref_particle_vertex(V, Pm, rad, scale, pos)
+        m = 2048
+        idx = rng.integers(0, pos.shape[0], m + EDGE_UV.shape[0])
+        uv = np.concatenate([rng.uniform(0.0, 1.0, size=(m, 2)).astype(np.float32), EDGE_UV])
+        color = rng.uniform(0.0, 1.0, size=(idx.size, 3)).astype(np.float32)
+        rgba_u, disc = O.ref_particle_fragment(rp, rad, eye[idx], uv)
+        rgba_c, disc_c = O.ref_particle_fragment(rp, rad, eye[idx], uv, color)
+        assert np.array_equal(disc, disc_c)
+        out.update({f"{name}_rp": np.frombuffer(bytes(rp), np.uint8).copy(),
+                    f"{name}_radius": np.array(radius, np.float32), f"{name}_pos": pos, f"{name}_eye": eye,
+                    f"{name}_size": size, f"{name}_clip": clip, f"{name}_frag_idx": idx.astype(np.int32),
+                    f"{name}_uv": uv, f"{name}_color": color, f"{name}_discarded": disc,
+                    f"{name}_rgba_uniform": rgba_u, f"{name}_rgba_color": rgba_c})
+    return out
+
+
 def main() -> None:
     O.build(force=True)
     if O.build_ref(sys.argv[1] if len(sys.argv) > 1 else None) is None:
@@ -117,6 +167,8 @@ def main() -> None:
         frames[f"{name}_substeps"] = sub
         frames[f"{name}_sim_times"] = times
     save_if_changed(os.path.join(HERE, "ref_frames.npz"), frames)
+
+    save_if_changed(os.path.join(HERE, "ref_shader.npz"), shader_cases())
 
     # oracle regression: 10x20x10 block, jitter-free, small box
     p = small_params()

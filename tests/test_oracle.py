@@ -1,6 +1,7 @@
 """The CPU oracle against the reference's golden vectors and against the
 mathematics it restates (CPU only)."""
 import hashlib
+import platform
 import os
 
 import numpy as np
@@ -229,3 +230,72 @@ def test_oracle_adaptive_substeps_reproduce_the_frames_fixture(oracle):
     _, k, dts = st.frames(p, 4, record_dts=20000)
     n = g["adaptive16k_dts"].size
     assert k >= n and np.array_equal(dts[:n].view(np.uint32), g["adaptive16k_dts"].view(np.uint32))
+
+
+def _shader_case(g, name):
+    rp = C.sf_render_params.from_buffer_copy(g[name + "_rp"].tobytes())
+    p = _cparams(float(g[name + "_radius"]))
+    return rp, p
+
+
+def _ulps(a, b):
+    """Largest distance in units in the last place between equal-shaped float32 arrays."""
+    ia = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    ib = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7FFFFFFF), ia)
+    ib = np.where(ib < 0, -(ib & 0x7FFFFFFF), ib)
+    return int(np.abs(ia - ib).max()) if ia.size else 0
+
+
+# The fixture was written on x86-64; the fragment colours go through the C
+# library's powf, which other hosts' libraries may round differently.
+POW_ULPS = 0 if platform.machine() in ("x86_64", "AMD64") else 2
+
+
+def test_oracle_shader_stages_match_the_reference_shaders(oracle):
+    """The oracle's restatement of the particle shaders (vertex: eye-space
+    centre, point size, clip position; fragment: discard test on the point
+    coordinate and Blinn-Phong over the lights) reproduces the reference's own
+    Shaders/particle.vs.glsl and particle.fs.glsl, compiled as C++ on seeded
+    particles and fragments (tests/golden/ref_shader.npz), bit for bit; two
+    settings (the viewer's, and eight lights with another camera) and both
+    uniform and per-particle colours."""
+    g = np.load(os.path.join(GOLD, "ref_shader.npz"))
+    for name in ("viewer", "lights8"):
+        rp, p = _shader_case(g, name)
+        eye, size, clip = oracle.particle_vertex(p, rp, g[name + "_pos"])
+        for got, key in ((eye, "_eye"), (size, "_size"), (clip, "_clip")):
+            assert np.array_equal(got.view(np.uint32), g[name + key].view(np.uint32)), name + key
+        fe, uv = eye[g[name + "_frag_idx"]], g[name + "_uv"]
+        keep = ~g[name + "_discarded"]
+        assert 0.1 < g[name + "_discarded"].mean() < 0.4 and keep[-8:].sum() == 6  # rim kept, corners not
+        for color, key in ((None, "_rgba_uniform"), (g[name + "_color"], "_rgba_color")):
+            rgba, disc = oracle.particle_fragment(p, rp, fe, uv, color)
+            assert np.array_equal(disc, g[name + "_discarded"]), name + key
+            assert _ulps(rgba[keep], g[name + key][keep]) <= POW_ULPS, name + key
+
+
+def test_oracle_shader_stages_against_the_reference_live(oracle):
+    """Where the reference's shaders are built here, compare on fresh inputs too."""
+    from simplefluid_gb300 import render_params
+    rp = render_params(width=800, height=600, eye=(-1.5, 2.0, 2.5), num_lights=3, mat_shininess=12.5)
+    for l in range(3):
+        rp.light_position[l][:] = [4.0 * l - 4.0, 6.0, 3.0 - l, 1.0]
+        rp.light_diffuse[l][:] = [0.3 + 0.2 * l, 0.5, 0.9 - 0.2 * l, 1.0]
+    p = _cparams(0.015)
+    V, Pm, scale, rad = oracle.render_camera(p, rp)
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(-1.2, 1.2, size=(300, 3)).astype(np.float32)
+    ref = oracle.ref_particle_vertex(V, Pm, rad, scale, pos)
+    if ref is None:
+        pytest.skip("the reference's shaders are not built on this machine")
+    got = oracle.particle_vertex(p, rp, pos)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    idx = rng.integers(0, 300, 1500)
+    uv = rng.uniform(-0.05, 1.05, size=(1500, 2)).astype(np.float32)
+    color = rng.uniform(0.0, 1.0, size=(1500, 3)).astype(np.float32)
+    rgba, disc = oracle.particle_fragment(p, rp, got[0][idx], uv, color)
+    rrgba, rdisc = oracle.ref_particle_fragment(rp, rad, got[0][idx], uv, color)
+    assert np.array_equal(disc, rdisc) and 0 < disc.sum() < disc.size
+    assert np.array_equal(rgba[~disc].view(np.uint32), rrgba[~rdisc].view(np.uint32))
