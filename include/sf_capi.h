@@ -134,9 +134,12 @@ SF_API sf_status sf_get_params(const sf_ctx* ctx, sf_params* p);
 /* ---- particle state: getParticles() / getVelocity() --------------------- */
 /* Copy a host AoS float3 state in (n * 3 floats each).  vel_xyz may be NULL
  * (zero velocity).  Page-locked arrays (sf_host_alloc) are copied by DMA, the
- * velocities while the positions are sorted.  Pageable arrays are read by the
- * GPU in place where it accesses pageable memory through the host's page
- * tables (Grace: NVLink-C2C), else staged through a page-locked buffer. */
+ * velocities while the positions are sorted; the call returns once both
+ * copies are done, with the sort still running on the context's stream
+ * (later calls queue behind it).  Pageable arrays are read by the GPU in place
+ * where it accesses pageable memory through the host's page tables (Grace:
+ * NVLink-C2C), else staged through a page-locked buffer.  Either way the
+ * caller may reuse its arrays once the call returns. */
 SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz, uint32_t n);
 /* Copy the state out in the caller's original particle order.  Either output
  * may be NULL.  Page-locked arrays are filled by DMA; pageable ones are

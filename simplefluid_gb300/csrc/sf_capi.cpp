@@ -226,6 +226,8 @@ sf_status alloc_grid(sf_ctx* ctx) {
 sf_status alloc_particles(sf_ctx* ctx, uint32_t n) {
     sf::DeviceState& d = ctx->d;
     if (n <= d.cap && d.pos) return SF_OK;
+    // queued work (a step, or the sort an upload left running) may still use the old buffers
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_trajectory(ctx);  // its buffers are sized by the capacity
     free_particles(d);
     const size_t c = n ? n : 1;
@@ -280,16 +282,21 @@ sf_status sort_uploaded(sf_ctx* ctx, const float* pos3, const float* vel3) {
     return SF_OK;
 }
 
+// The second stream and its events, made on first use.
+sf_status need_aux(sf_ctx* ctx) {
+    if (!ctx->aux) SF_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    for (cudaEvent_t* ev : {&ctx->ev_pos, &ctx->ev_vel, &ctx->ev_in, &ctx->ev_out})
+        if (!*ev) SF_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    return SF_OK;
+}
+
 // Upload from page-locked host arrays: positions first, then the velocity
 // copy on the second stream while the positions are hashed, counted and
-// scattered; the gather waits for the velocities.
+// scattered; the gather waits for the velocities.  ev_in marks the end of
+// both copies (the velocity copy starts after the position copy).
 sf_status upload_overlapped(sf_ctx* ctx, const float* pos_xyz, const float* vel_xyz) {
     sf::DeviceState& d = ctx->d;
-    if (!ctx->aux) {
-        SF_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
-        SF_CUDA(cudaEventCreateWithFlags(&ctx->ev_pos, cudaEventDisableTiming));
-        SF_CUDA(cudaEventCreateWithFlags(&ctx->ev_vel, cudaEventDisableTiming));
-    }
+    SF_TRY(need_aux(ctx));
     const size_t bytes = (size_t)d.n * 3 * sizeof(float);
     float* io_pos = d.io;
     float* io_vel = d.io + 3 * (size_t)d.n;
@@ -297,6 +304,7 @@ sf_status upload_overlapped(sf_ctx* ctx, const float* pos_xyz, const float* vel_
     SF_CUDA(cudaEventRecord(ctx->ev_pos, ctx->stream));
     SF_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->ev_pos, 0));  // after all earlier work on io
     SF_CUDA(cudaMemcpyAsync(io_vel, vel_xyz, bytes, cudaMemcpyHostToDevice, ctx->aux));
+    SF_CUDA(cudaEventRecord(ctx->ev_in, ctx->aux));
     sf::launch_load_vel(io_vel, d.n, d.vel2, ctx->aux);
     SF_CUDA(cudaEventRecord(ctx->ev_vel, ctx->aux));
     sf::launch_load_pos(io_pos, d.n, d.pos2, ctx->stream);
@@ -409,9 +417,10 @@ void release_ctx(sf_ctx* ctx) {
     ctx->h_stage = nullptr;
     if (ctx->d_report) cudaFree(ctx->d_report);
     ctx->d_report = nullptr;
-    if (ctx->ev_pos) cudaEventDestroy(ctx->ev_pos);
-    if (ctx->ev_vel) cudaEventDestroy(ctx->ev_vel);
-    ctx->ev_pos = ctx->ev_vel = nullptr;
+    for (cudaEvent_t* ev : {&ctx->ev_pos, &ctx->ev_vel, &ctx->ev_in, &ctx->ev_out}) {
+        if (*ev) cudaEventDestroy(*ev);
+        *ev = nullptr;
+    }
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
     ctx->aux = nullptr;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -730,7 +739,9 @@ SF_API sf_status sf_set_state(sf_ctx* ctx, const float* pos_xyz, const float* ve
     if (n == 0) return SF_OK;
     if (vel_xyz && is_pinned(pos_xyz) && is_pinned(vel_xyz)) {
         SF_TRY(upload_overlapped(ctx, pos_xyz, vel_xyz));
-        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        // The caller's arrays are read once both copies end; the sort goes on
+        // on the stream, and the next call queues behind it.
+        SF_CUDA(cudaEventSynchronize(ctx->ev_in));
         return SF_OK;
     }
     if (host_direct(ctx, pos_xyz) && (!vel_xyz || host_direct(ctx, vel_xyz))) {
@@ -763,6 +774,22 @@ SF_API sf_status sf_get_state(sf_ctx* ctx, float* pos_xyz, float* vel_xyz, uint3
     }
     float* io = ctx->d.io;
     const size_t bytes = (size_t)n * 3 * sizeof(float);
+    if (pos_xyz && vel_xyz && is_pinned(pos_xyz) && is_pinned(vel_xyz)) {
+        // page-locked outputs: positions stored and copied on the stream, the
+        // velocities on the second stream meanwhile; one wait for both
+        SF_TRY(need_aux(ctx));
+        SF_CUDA(cudaEventRecord(ctx->ev_out, ctx->stream));
+        SF_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->ev_out, 0));
+        sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, io, nullptr, ctx->stream);
+        sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, nullptr, io + 3 * (size_t)n, ctx->aux);
+        SF_TRY(check_launch("store state"));
+        SF_CUDA(cudaMemcpyAsync(pos_xyz, io, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        SF_CUDA(cudaMemcpyAsync(vel_xyz, io + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost, ctx->aux));
+        SF_CUDA(cudaEventRecord(ctx->ev_out, ctx->aux));
+        SF_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_out, 0));  // later work waits for the velocity reads
+        SF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return SF_OK;
+    }
     sf::launch_store_aos(ctx->d.pos, ctx->d.vel, n, pos_xyz ? io : nullptr, vel_xyz ? io + 3 * (size_t)n : nullptr,
                          ctx->stream);
     SF_TRY(check_launch("store state"));

@@ -61,7 +61,7 @@ struct sf_ctx {
     cudaStream_t stream = nullptr;
     // uploads: a second stream, so that the velocity copy overlaps the sort
     cudaStream_t aux = nullptr;
-    cudaEvent_t ev_pos = nullptr, ev_vel = nullptr;
+    cudaEvent_t ev_pos = nullptr, ev_vel = nullptr, ev_in = nullptr, ev_out = nullptr;
     // the GPU reads and writes pageable host memory through the host's page
     // tables (Grace: NVLink-C2C with address translation): -1 unknown, 0, 1
     int host_direct = -1;

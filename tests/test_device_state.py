@@ -190,3 +190,50 @@ def test_pinned_host_upload_matches_pageable(lib):
     finally:
         lib.sf_host_free(hp)
         lib.sf_host_free(hv)
+
+
+@pytest.mark.gpu
+def test_pinned_upload_returns_before_its_sort_finishes(lib):
+    """sf_set_state from page-locked arrays returns once the copies are done and
+    leaves the sort queued.  What comes next must still see the sorted upload:
+    an immediate page-locked read (stores split over two streams) returns the
+    arrays unchanged, the caller may overwrite its arrays at once, and a larger
+    upload (which reallocates the buffers the queued sort uses) gives the same
+    state as a fresh context."""
+    prm, pos, vel = _scene()
+    n = pos.shape[0]
+    hp, hv = ctypes.c_void_p(), ctypes.c_void_p()
+    C.check(lib.sf_host_alloc(n * 12, ctypes.byref(hp)))
+    C.check(lib.sf_host_alloc(n * 12, ctypes.byref(hv)))
+    try:
+        P = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hp.value)).reshape(n, 3)
+        V = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hv.value)).reshape(n, 3)
+        with SPHSolver(prm) as s:
+            for _ in range(3):
+                P[:] = pos
+                V[:] = vel
+                C.check(lib.sf_set_state(s.handle, hp, hv, n))
+                P[:] = np.nan  # the upload has been read: overwriting is allowed
+                V[:] = np.nan
+                C.check(lib.sf_get_state(s.handle, hp, hv, n))
+                assert np.array_equal(P.view(np.uint32), pos.view(np.uint32))
+                assert np.array_equal(V.view(np.uint32), vel.view(np.uint32))
+            P[:] = pos
+            V[:] = vel
+            C.check(lib.sf_set_state(s.handle, hp, hv, n))
+            big_p = np.concatenate([pos, pos[: n // 2] * np.float32(0.5) + np.float32(0.25)])
+            big_v = np.concatenate([vel, vel[: n // 2]])
+            s.setParticles(big_p, big_v)  # grows the buffers right behind the queued sort
+            s.makeReady()
+            s.step(5)
+            got = s.getState()
+        with SPHSolver(prm) as f:
+            f.setParticles(big_p, big_v)
+            f.makeReady()
+            f.step(5)
+            ref = f.getState()
+        for x, y in zip(got, ref):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    finally:
+        lib.sf_host_free(hp)
+        lib.sf_host_free(hv)
