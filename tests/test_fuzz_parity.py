@@ -12,8 +12,11 @@ It then builds a particle set from several parts:
   * a dense cluster that overflows the neighbour lists;
   * particles on the box faces and corners, and some outside the box.
 A few sub-steps run on both sides.  The caller-order positions and velocities
-must match bit for bit.
-The generator itself is checked on the CPU: every case passes
+must match bit for bit, under every neighbour-list layout.  Batches of eight
+such scenes (fixed time step, one grid granularity per batch, some with an
+empty scene) run under the five-launch and the persistent batched step and
+must match the oracle run on each scene alone.
+The generators themselves are checked on the CPU: every case passes
 sf_params_update.
 """
 import numpy as np
@@ -91,3 +94,100 @@ def test_random_case_bit_identical(seed, oracle):
         gpos, gvel = s.getState()
     assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
     assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32))
+
+
+def _with_list_mode(lib, s, mode):
+    import ctypes
+    t = C.sf_tuning()
+    C.check(lib.sf_get_tuning(s.handle, ctypes.byref(t)))
+    t.list_mode = mode
+    C.check(lib.sf_set_tuning(s.handle, ctypes.byref(t)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(CASES))
+def test_random_case_every_list_mode(seed, oracle, lib):
+    """The same random cases with the other neighbour-list layouts (none,
+    shared-memory staged, 16-bit warp tiles): every layout gives the
+    oracle's bits."""
+    prm, pos, vel = make_case(seed)
+    st = oracle.State(pos, vel)
+    st.step(prm.to_c(), STEPS)
+    opos, ovel = st.original_order()
+    for mode in (C.SF_LIST_NONE, C.SF_LIST_TILE_STAGED, C.SF_LIST_TILE16):
+        with SPHSolver(prm) as s:
+            s.setParticles(pos, vel)
+            _with_list_mode(lib, s, mode)
+            s.makeReady()
+            s.step(STEPS)
+            gpos, gvel = s.getState()
+        assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32)), mode
+        assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32)), mode
+
+
+def make_batch(index: int, K: int):
+    """Eight random cases (fixed time step, all at grid granularity K) for one
+    batch; every third batch has an empty scene."""
+    params, poss, vels = [], [], []
+    seed = 5000 + 100 * index
+    while len(params) < 8:
+        prm, pos, vel = make_case(seed)
+        seed += 1
+        if prm.cellsPerH < K:  # its grid was sized for a coarser K
+            continue
+        prm.adaptiveTimeStep = False
+        prm.cellsPerH = K
+        params.append(prm.to_c())
+        poss.append(pos)
+        vels.append(vel)
+    if index % 3 == 0:
+        poss[3], vels[3] = poss[3][:0], vels[3][:0]
+    return params, poss, vels
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("index", range(6))
+def test_random_batch_every_step_form(index, oracle):
+    """Batches of random scenes (their own boxes, radii, EOS and parameters)
+    under the five-launch step with 32- and 16-bit lists and under the
+    persistent cluster step: each scene gives the oracle's bits."""
+    from simplefluid_gb300 import SPHBatch
+    K = 2 if index % 2 == 0 else 1
+    params, poss, vels = make_batch(index, K)
+    counts = np.array([p.shape[0] for p in poss], np.uint32)
+    pos = np.concatenate(poss).astype(np.float32)
+    vel = np.concatenate(vels).astype(np.float32)
+    refs = []
+    for s in range(len(params)):
+        if counts[s] == 0:
+            refs.append((poss[s], vels[s]))
+            continue
+        st = oracle.State(poss[s], vels[s])
+        st.step(params[s], STEPS)
+        st.sort(params[s])
+        refs.append(st.original_order())
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    tunings = [(C.SF_LIST_TILE, 128, 128, 2, 0, 0, 0), (C.SF_LIST_TILE16, 128, 128, 2, 0, 0, 0),
+               (C.SF_LIST_TILE, 256, 128, 2, 0, 4, 256), (C.SF_LIST_TILE, 256, 128, 2, 0, 8, 1024),
+               (C.SF_LIST_TILE, 256, 128, 2, 0, 2, 512)]
+    for tune in tunings:
+        with SPHBatch(params) as b:
+            b.setState(counts, pos, vel)
+            b.setTuning(C.sf_tuning(*tune))
+            b.step(STEPS)
+            gpos, gvel = b.getState()
+        for s in range(len(params)):
+            sl = slice(int(off[s]), int(off[s + 1]))
+            assert np.array_equal(gpos[sl].view(np.uint32), refs[s][0].view(np.uint32)), (tune, s)
+            assert np.array_equal(gvel[sl].view(np.uint32), refs[s][1].view(np.uint32)), (tune, s)
+
+
+@pytest.mark.parametrize("index", range(6))
+def test_random_batch_is_valid(index, lib):
+    import ctypes
+    K = 2 if index % 2 == 0 else 1
+    params, poss, _ = make_batch(index, K)
+    for p in params:
+        assert p.cells_per_h == K and not p.adaptive_time_step
+        assert lib.sf_params_update(ctypes.byref(p)) == C.SF_OK, C.load().sf_last_error()
+    assert sum(x.shape[0] for x in poss) > 400
