@@ -15,7 +15,8 @@ A few sub-steps run on both sides.  The caller-order positions and velocities
 must match bit for bit, under every neighbour-list layout.  Batches of eight
 such scenes (fixed time step, one grid granularity per batch, some with an
 empty scene) run under the five-launch and the persistent batched step and
-must match the oracle run on each scene alone.
+must match the oracle run on each scene alone.  The adjoint of each random
+case (fixed time step) must match the oracle's FP32 adjoint.
 The generators themselves are checked on the CPU: every case passes
 sf_params_update.
 """
@@ -191,3 +192,30 @@ def test_random_batch_is_valid(index, lib):
         assert p.cells_per_h == K and not p.adaptive_time_step
         assert lib.sf_params_update(ctypes.byref(p)) == C.SF_OK, C.load().sf_last_error()
     assert sum(x.shape[0] for x in poss) > 400
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(CASES))
+def test_random_case_adjoint_matches_fp32_oracle(seed, oracle):
+    """The adjoint (sf_forward + sf_adjoint) on the random cases, with a fixed
+    time step, from a seeded final-state adjoint of positions and velocities:
+    the GPU gradients of the initial state equal the FP32 oracle adjoint's bit
+    for bit, and the viscosity and stiffness gradients agree to the rounding
+    of their reductions."""
+    prm, pos, vel = make_case(seed)
+    prm.adaptiveTimeStep = False
+    rng = np.random.default_rng(77 + seed)
+    steps, ckpt = 6, 3
+    sx = rng.normal(size=pos.shape).astype(np.float32)
+    sv = rng.normal(size=pos.shape).astype(np.float32)
+    with SPHSolver(prm) as s:
+        s.setParticles(pos, vel)
+        s.forward(steps, ckpt)
+        pf = s.getState()[0]
+        dx0, dv0, dmu, dk = s.adjoint(sx, sv)
+    ox, ov, om, ok, opf = oracle.adjoint(prm.to_c(), pos, vel, steps, sx, sv, ckpt=ckpt, dtype=np.float32)
+    assert np.array_equal(pf.view(np.uint32), opf.view(np.uint32))
+    assert np.array_equal(dx0.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(dv0.view(np.uint32), ov.view(np.uint32))
+    assert dmu == pytest.approx(om, rel=1e-5, abs=1e-30)
+    assert dk == pytest.approx(ok, rel=1e-5, abs=1e-30)
