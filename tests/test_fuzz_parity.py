@@ -16,7 +16,8 @@ must match bit for bit, under every neighbour-list layout.  Batches of eight
 such scenes (fixed time step, one grid granularity per batch, some with an
 empty scene) run under the five-launch and the persistent batched step and
 must match the oracle run on each scene alone.  The adjoint of each random
-case (fixed time step) must match the oracle's FP32 adjoint.
+case (fixed time step) must match the oracle's FP32 adjoint, and whole
+frames on the device must match the oracle's frame loop.
 The generators themselves are checked on the CPU: every case passes
 sf_params_update.
 """
@@ -219,3 +220,25 @@ def test_random_case_adjoint_matches_fp32_oracle(seed, oracle):
     assert np.array_equal(dv0.view(np.uint32), ov.view(np.uint32))
     assert dmu == pytest.approx(om, rel=1e-5, abs=1e-30)
     assert dk == pytest.approx(ok, rel=1e-5, abs=1e-30)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(0, CASES, 2))
+def test_random_case_frames_on_device(seed, oracle):
+    """Whole frames on the device (the conditional-graph frame loop) on the
+    random cases: sub-step count, simulated time and state equal the oracle's
+    frame loop.  Frames of 1.5 ms hold a few to a few dozen sub-steps of the
+    cases' fixed or adaptive step."""
+    prm, pos, vel = make_case(seed)
+    frame_time, frames, cap = 1.5e-3, 2, 200
+    with SPHSolver(prm) as s:
+        s.setParticles(pos, vel)
+        t, k = s.advanceFrames(frames, frame_time, cap)
+        gpos, gvel = s.getState()
+    st = oracle.State(pos, vel)
+    ot, ok, _ = st.frames(prm.to_c(), frames, frame_time=frame_time, max_substeps=cap)
+    assert k == ok and t == ot and k >= frames
+    st.sort(prm.to_c())
+    opos, ovel = st.original_order()
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(gvel.view(np.uint32), ovel.view(np.uint32))
