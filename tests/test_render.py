@@ -60,3 +60,55 @@ def test_render_rejects_bad_parameters():
         for kw in (dict(width=0), dict(num_lights=9), dict(color_mode=5), dict(fovy_deg=0.0)):
             with pytest.raises(C.SFError):
                 s.render(render_params(**kw))
+
+
+def _random_view(seed: int):
+    """A seeded camera, light set, material and colour mode around the unit box."""
+    rng = np.random.default_rng(300 + seed)
+    d = rng.normal(size=3)
+    eye = 0.5 + d / np.linalg.norm(d) * rng.uniform(1.2, 4.0)
+    rp = render_params(width=int(rng.integers(64, 400)), height=int(rng.integers(64, 300)),
+                       eye=tuple(eye), focus=tuple(rng.uniform(0.3, 0.7, 3)), fovy_deg=float(rng.uniform(30, 80)),
+                       point_radius=float(rng.choice([0.0, rng.uniform(0.005, 0.05)])),
+                       num_lights=int(rng.integers(1, 9)), mat_shininess=float(rng.uniform(1, 300)),
+                       color_mode=int(rng.integers(0, 3)), color_seed=int(rng.integers(0, 2 ** 32)))
+    for l in range(8):
+        rp.light_position[l][:] = [*rng.uniform(-10, 10, 3), 1.0]
+        rp.light_ambient[l][:] = [*rng.uniform(0, 0.2, 3), 1.0]
+        rp.light_diffuse[l][:] = [*rng.uniform(0, 1, 3), 1.0]
+        rp.light_specular[l][:] = [*rng.uniform(0, 1, 3), 1.0]
+    rp.mat_ambient[:] = [*rng.uniform(0, 1, 3), 1.0]
+    rp.mat_diffuse[:] = [*rng.uniform(0, 1, 3), 1.0]
+    rp.mat_specular[:] = [*rng.uniform(0, 1, 3), 1.0]
+    return rp
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(12))
+def test_render_random_views_match_oracle(oracle, seed):
+    """Seeded cameras, lights, materials, point radii and colour modes over a
+    random particle set: visibility and depth bit-identical to the oracle,
+    colours within 1e-4 relative."""
+    rng = np.random.default_rng(seed)
+    prm = params_16k()
+    pos = np.concatenate([rng.uniform(0.0, 1.0, size=(3000, 3)),
+                          0.5 + rng.normal(scale=0.05, size=(1000, 3))]).astype(np.float32)
+    rp = _random_view(seed)
+    with SPHSolver(prm) as s:
+        s.setParticles(pos)
+        state, _ = s.getState()
+        rgba, depth, owner = s.render(rp)
+    orgba, odepth, oowner = oracle.render(prm.to_c(), rp, state)
+    assert np.array_equal(owner, oowner)
+    assert np.array_equal(depth.view(np.uint32), odepth.view(np.uint32))
+    assert np.all(np.abs(rgba - orgba) <= 1e-4 * np.maximum(1.0, np.abs(orgba)))
+
+
+def test_random_views_are_valid():
+    modes = set()
+    for seed in range(12):
+        rp = _random_view(seed)
+        assert 1 <= rp.num_lights <= 8 and rp.width >= 64 and rp.height >= 64
+        assert 30.0 <= rp.fovy_deg <= 80.0 and rp.znear > 0.0 and rp.zfar > rp.znear
+        modes.add(rp.color_mode)
+    assert modes == {C.SF_COLOR_UNIFORM, C.SF_COLOR_RANDOM, C.SF_COLOR_RAMP}
