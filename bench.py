@@ -14,7 +14,8 @@ Printed JSON line (rank 0):
              a cold L2.
   e2e        the same metric through the C ABI with host buffers: per step
              sf_set_state (pinned host AoS pos+vel -> device) + sf_advance_frame
-             + sf_get_state (device -> pinned host), wall clock.
+             + sf_get_state (device -> pinned host), wall clock; parts_ms
+             gives each call's own time (synchronised, medians of 10).
   roofline   the dominant kernel's algorithmic bytes per launch / its average
              launch time (CUDA events between stages over K profiled steps),
              against the measured HBM copy bandwidth.
@@ -658,6 +659,24 @@ def run_ours(args, workload):
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
     finite = bool(np.isfinite(pos_h).all() and np.isfinite(vel_h).all())
+    # where an end-to-end step's time goes: each call on its own, synchronised
+    # (medians of 10; the upload returns when its copies end, its sort after)
+    parts = {"set_state_return": [], "set_state": [], "advance_frame": [], "get_state": []}
+    for _ in range(10):
+        t1 = time.perf_counter()
+        C.check(lib.sf_set_state(ctx, hp, hv, n))
+        t2 = time.perf_counter()
+        C.check(lib.sf_synchronize(ctx))
+        t3 = time.perf_counter()
+        C.check(lib.sf_advance_frame(ctx, ctypes.byref(dtv)))
+        C.check(lib.sf_synchronize(ctx))
+        t4 = time.perf_counter()
+        C.check(lib.sf_get_state(ctx, hp, hv, n))
+        t5 = time.perf_counter()
+        for k, dt_ in (("set_state_return", t2 - t1), ("set_state", t3 - t1), ("advance_frame", t4 - t3),
+                       ("get_state", t5 - t4)):
+            parts[k].append(dt_ * 1e3)
+    e2e_parts = {k: statistics.median(v) for k, v in parts.items()}
     lib.sf_host_free(hp)
     lib.sf_host_free(hv)
     e2e_value = ws * n * e2e_steps / e2e_s
@@ -701,7 +720,7 @@ def run_ours(args, workload):
         "stages_ms": avg_ms,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
                 "path": "sf_set_state(pinned host) + sf_advance_frame + sf_get_state(pinned host)",
-                "state_finite": finite},
+                "state_finite": finite, "parts_ms": e2e_parts},
         "gpu_launches": kernels_per_step * args.steps,
         "tuning": args.tuning,
         "pre_steps": args.pre_steps,

@@ -39,6 +39,9 @@ def test_our_arm_line():
     e = d["e2e"]
     assert e["unit"] == d["unit"] and e["h2d_bytes_per_step"] == 2 * n * 12 and e["d2h_bytes_per_step"] == 2 * n * 12
     assert 0 < e["value"] < d["value"] and e["state_finite"]
+    parts = e["parts_ms"]
+    assert 0 < parts["set_state_return"] <= parts["set_state"] and parts["advance_frame"] > 0
+    assert parts["get_state"] > 0
     c = d["cpu_baseline"]
     assert c["kind"] == "port" and c["cores"] >= 1 and c["value"] > 0
     assert d["gpu_launches"] == 5 * d["steps"]
