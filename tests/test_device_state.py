@@ -237,3 +237,59 @@ def test_pinned_upload_returns_before_its_sort_finishes(lib):
     finally:
         lib.sf_host_free(hp)
         lib.sf_host_free(hv)
+
+
+@pytest.mark.gpu
+def test_pinned_download_after_each_kind_of_state_change(lib):
+    """A page-locked sf_get_state (stores and copies split over two streams)
+    gives the pageable read's bits after every kind of change of the state:
+    steps, a parameter change that re-buckets the state, whole frames, a
+    write through the device view and a forward/adjoint pair."""
+    torch = pytest.importorskip("torch")
+    prm, pos, vel = _scene()
+    n = pos.shape[0]
+    hp, hv = ctypes.c_void_p(), ctypes.c_void_p()
+    C.check(lib.sf_host_alloc(n * 12, ctypes.byref(hp)))
+    C.check(lib.sf_host_alloc(n * 12, ctypes.byref(hv)))
+    try:
+        P = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hp.value)).reshape(n, 3)
+        V = np.ctypeslib.as_array((ctypes.c_float * (3 * n)).from_address(hv.value)).reshape(n, 3)
+
+        def pinned_equals_pageable(s):
+            P[:] = np.nan
+            V[:] = np.nan
+            C.check(lib.sf_get_state(s.handle, hp, hv, n))
+            p2, v2 = s.getState()
+            assert np.array_equal(P.view(np.uint32), p2.view(np.uint32))
+            assert np.array_equal(V.view(np.uint32), v2.view(np.uint32))
+            return p2
+
+        with SPHSolver(prm) as s:
+            s.setParticles(pos, vel)
+            s.makeReady()
+            for k in (1, 7):
+                s.step(k)
+                pinned_equals_pageable(s)
+            s.setParams(params_16k(viscosity=0.02, kernelRadius=0.05))  # a new grid: the state is re-bucketed
+            pinned_equals_pageable(s)
+            s.step(3)
+            s.advanceFrames(1, 2e-3, 40)
+            pinned_equals_pageable(s)
+            s.step(2)
+            before = pinned_equals_pageable(s)
+            v = s.deviceState()  # shift every x by 1e-3 through the view
+            pos4 = torch.as_tensor(_Cai(v.pos4, (v.n, 4)), device="cuda")
+            torch.cuda.synchronize()
+            pos4[:, 0] += 1e-3
+            torch.cuda.synchronize()
+            after = pinned_equals_pageable(s)
+            assert np.array_equal(after[:, 0], before[:, 0] + np.float32(1e-3))
+            s.step(1)
+            pinned_equals_pageable(s)
+            s.forward(4, 2)
+            pinned_equals_pageable(s)
+            s.adjoint(np.ones((n, 3), np.float32))
+            pinned_equals_pageable(s)
+    finally:
+        lib.sf_host_free(hp)
+        lib.sf_host_free(hv)
