@@ -233,6 +233,16 @@ class SPHSolver:
         C.check(self._lib.sf_check_state(self._ctx, byref(r)))
         return r.as_dict()
 
+    def setTuning(self, t: C.sf_tuning) -> None:
+        """Kernel choices of this solver's step (sf_set_tuning); every choice
+        computes the same bits."""
+        C.check(self._lib.sf_set_tuning(self._ctx, byref(t)))
+
+    def getTuning(self) -> C.sf_tuning:
+        t = C.sf_tuning()
+        C.check(self._lib.sf_get_tuning(self._ctx, byref(t)))
+        return t
+
     def deviceState(self) -> "C.sf_device_view":
         """Device pointers to the cell-sorted working arrays (sf_device_view)."""
         v = C.sf_device_view()

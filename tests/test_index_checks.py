@@ -3,8 +3,10 @@ cell-table range end and neighbour-list entry before use and count bad ones.
 
 * CPU: the release library reports that it has no checks and counts nothing.
 * GPU: the checked library, run through the candidate walks, the list and
-  rescan paths of the force pass, a batch and the adjoint, counts no bad index
-  and gives the release library's bits.
+  rescan paths of the force pass under every list layout, a batch under the
+  five-launch and the persistent step, whole frames with the adaptive
+  sub-step and the adjoint, counts no bad index and gives the release
+  library's bits.
 """
 import json
 import os
@@ -49,6 +51,32 @@ with SPHBatch(params) as b:
     b.step(5)
     bp, bv = b.getState()
     h.update(bp.tobytes()); h.update(bv.tobytes())
+# the other neighbour-list layouts (none, staged, 16-bit warp tiles), on the
+# scene and on the overflowing cluster
+for mode in (0, 1, 3):
+    for pts in (pos, cl):
+        with SPHSolver(prm) as s:
+            s.setParticles(pts)
+            t = s.getTuning()
+            t.list_mode = mode
+            s.setTuning(t)
+            s.step(4)
+            p, v = s.getState()
+            h.update(p.tobytes()); h.update(v.tobytes())
+# the persistent batched step
+with SPHBatch(params) as b:
+    b.setState(counts, bpos)
+    b.setTuning(C.sf_tuning(C.SF_LIST_TILE, 256, 128, 2, 0, 4, 256))
+    b.step(5)
+    bp, bv = b.getState()
+    h.update(bp.tobytes()); h.update(bv.tobytes())
+# whole frames with the adaptive sub-step
+aprm = SPHParameters(particleRadius=0.01, kernelRadius=0.04, scene=16, adaptiveTimeStep=True, timeStep=2e-3)
+with SPHSolver(aprm) as s:
+    s.setParticles(pos)
+    t_sim, k = s.advanceFrames(1, 4e-3, 60)
+    p, v = s.getState()
+    h.update(p.tobytes()); h.update(v.tobytes()); h.update(np.array([t_sim, k]).tobytes())
 # the adjoint (recorded lists, rescans, reverse sweep)
 sub = pos[:4000]
 vel = np.random.default_rng(5).normal(scale=0.05, size=sub.shape).astype(np.float32)
